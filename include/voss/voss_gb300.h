@@ -1,0 +1,134 @@
+/* voss_gb300.h -- additions to the voss C ABI made by the GB300 build.
+ *
+ * Everything here is additive: the reference has no counterpart for range
+ * statistics over an arbitrary [a, b), batches, reusable launch plans, the
+ * smallest-Goldbach-prime output or the request server.  The reference
+ * functions these build on are cited per entry.  All functions return a
+ * VOSS_* code from voss.h and set voss_get_last_error() on failure.
+ */
+#ifndef VOSS_GB300_H
+#define VOSS_GB300_H
+
+#include <stdint.h>
+#include "voss/voss.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Gap histogram of a range, indexed by gap/2: bin 0 is the gap 1 (2 -> 3),
+ * bin i (1 <= i <= 200) the gap 2i, bin 201 every gap above 400. */
+#define VOSS_GAP_BINS 202
+/* The full histogram: bins 0..1023 as above (gaps up to 2046), bin 1024
+ * every gap >= 2048. */
+#define VOSS_GAP_BINS_FULL 1025
+
+/* Statistics of the primes q with a <= q < b.  Gaps are between consecutive
+ * primes that both lie in [a, b).  twins/cousins/sexy count gaps of 2/4/6
+ * between consecutive primes, as the reference's ctx_twins/cousin/sexy do
+ * (context.cu:965-975).  Chebyshev classes: pi_4_1 / pi_4_3 primes = 1 / 3
+ * mod 4 (2 in neither), pi_3_1 / pi_3_2 primes = 1 / 2 mod 3 (3 in neither).
+ * max_gap_start is the first prime of the earliest largest gap.
+ * large_gaps counts gaps >= 500 (the reference's threshold, context.cu:64). */
+typedef struct {
+    uint64_t a, b;
+    uint64_t count;
+    uint64_t twins, cousins, sexy;
+    uint64_t pi_4_1, pi_4_3, pi_3_1, pi_3_2;
+    uint64_t first_prime, last_prime;      /* 0 if there is no prime */
+    uint64_t max_gap, max_gap_start;       /* 0 if fewer than two primes */
+    uint64_t num_gaps;
+    uint64_t large_gaps;
+    uint64_t gap_hist[VOSS_GAP_BINS];
+} voss_range_stats_t;
+
+/* One range [a, b), b <= 10^14 + 10^10 + 1.  Replaces the reference's
+ * in_range_with_limit + host reduction for offset ranges (range.cu:99-262). */
+int voss_primes_range_stats(uint64_t a, uint64_t b, voss_range_stats_t* out);
+
+/* As above, plus the full gap/2 histogram (VOSS_GAP_BINS_FULL entries) when
+ * hist_full is not NULL. */
+int voss_primes_range_stats_ex(uint64_t a, uint64_t b, voss_range_stats_t* out,
+                               uint64_t* hist_full);
+
+/* n independent ranges in one launch (one persistent kernel over all their
+ * segments).  out[i] is the result of [a[i], b[i]). */
+int voss_primes_range_stats_batch(uint64_t n, const uint64_t* a, const uint64_t* b,
+                                  voss_range_stats_t* out);
+
+/* Tunables of the segmented sieve.  seg_bytes: shared-memory segment in
+ * bytes (30 integers each), a multiple of 128, at most 196608.  threads: CTA
+ * size (multiple of 32, <= 1024).  tier_split: primes below it are marked a
+ * warp per prime, primes above it a thread per prime.  ctas_per_sm: resident
+ * CTAs per SM used to size the persistent grid.  Zero fields keep the
+ * current value; auto_tune = 1 lets the library pick per range. */
+typedef struct {
+    uint32_t seg_bytes;
+    uint32_t threads;
+    uint32_t tier_split;
+    uint32_t ctas_per_sm;
+    uint32_t auto_tune;
+} voss_gb300_config_t;
+
+int voss_gb300_get_config(voss_gb300_config_t* out);
+int voss_gb300_set_config(const voss_gb300_config_t* cfg);
+
+/* A launch plan: the requests, their segment list and all device buffers,
+ * prepared once and launched any number of times on a caller's stream (also
+ * inside stream capture, after the first launch).  Used to time the device
+ * part alone and by the request server. */
+typedef struct voss_gb300_plan voss_gb300_plan;
+
+int voss_gb300_plan_create(uint64_t n, const uint64_t* a, const uint64_t* b,
+                           voss_gb300_plan** out);
+/* Enqueue one full run (reset, sieve, finalize) on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream).  Does not synchronise. */
+int voss_gb300_plan_launch(voss_gb300_plan* plan, void* stream);
+/* Copy the results of the last run to the host (synchronises `stream`). */
+int voss_gb300_plan_results(voss_gb300_plan* plan, voss_range_stats_t* out, void* stream);
+/* Segments, grid size, kernels per run, shared bytes per CTA, and the
+ * algorithmic work of one run: candidate clears by primes >= 37, and the
+ * wheel bytes covered. */
+int voss_gb300_plan_info(voss_gb300_plan* plan, uint64_t* total_segments, uint32_t* grid,
+                         uint32_t* kernels_per_run, uint32_t* smem_bytes,
+                         uint64_t* clears, uint64_t* wheel_bytes);
+void voss_gb300_plan_free(voss_gb300_plan* plan);
+/* Durations in ms of the sieve kernel and the finalize kernel of the plan's
+ * last launch, from CUDA events recorded on the launching stream (waits for
+ * that launch to finish). */
+int voss_gb300_plan_kernel_ms(voss_gb300_plan* plan, float* sieve_ms, float* finalize_ms);
+
+/* Every even n in [4, N], N <= 4*10^11: the smallest prime p with n - p prime
+ * (the p at which the reference's goldbach_check_kernel stops,
+ * goldbach_upto.cu:38-43; the reference does not output it).
+ * minp: NULL or (N-4)/2+1 entries, minp[(n-4)/2] = p, 0 for a counterexample.
+ * hist: NULL or VOSS_GOLDBACH_HIST_BINS entries, hist[p] = number of n.
+ * max_minp, sum_minp, n_counterexamples: NULL or outputs. */
+#define VOSS_GOLDBACH_HIST_BINS 65536
+int voss_primes_goldbach_minp(uint64_t N, uint32_t* minp, uint64_t* hist,
+                              uint32_t* max_minp, uint64_t* sum_minp,
+                              uint64_t* n_counterexamples);
+
+/* Device-resident Goldbach run (sieve, odd-number bitmap, min-p kernel) that
+ * can be launched repeatedly on a stream; used to time the device part. */
+typedef struct voss_gb300_goldbach voss_gb300_goldbach;
+int voss_gb300_goldbach_create(uint64_t N, voss_gb300_goldbach** out);
+int voss_gb300_goldbach_launch(voss_gb300_goldbach* g, void* stream);
+int voss_gb300_goldbach_results(voss_gb300_goldbach* g, uint32_t* max_minp,
+                                uint64_t* sum_minp, uint64_t* n_counterexamples,
+                                uint64_t* hist, uint64_t* probes, void* stream);
+void voss_gb300_goldbach_free(voss_gb300_goldbach* g);
+
+/* Shared-memory bandwidth of this GPU in GB/s, measured by two
+ * microbenchmarks (conflict-free 32-bit load+store, and atomicAnd; 8 bytes
+ * per step each): the denominators of the sieve's roofline. */
+int voss_gb300_smem_peak(double* ldst_gbs, double* atomic_gbs);
+
+/* Name of the device the library runs on, and its SM count. */
+int voss_gb300_device_info(char* name, uint32_t name_len, uint32_t* sm_count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VOSS_GB300_H */

@@ -1,0 +1,248 @@
+"""Parity of the GB300 sieve with the oracle and the reference's golden values.
+
+Integer results must be bit-exact.  Statistics (host doubles, the reference's
+loop order) must equal the oracle's restatement exactly and the reference
+oracle's within 1e-9 relative (the reference's own check uses 1e-4 absolute,
+verify_against_reference.py:146).
+"""
+import random
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+EXACT_KEYS = ("count", "pi_4_1", "pi_4_3", "pi_3_1", "pi_3_2", "max_gap", "max_gap_start", "num_gaps")
+
+
+def assert_range_equal(st, orc, ctx=""):
+    for k in EXACT_KEYS:
+        assert getattr(st, k) == orc[k], (ctx, k, getattr(st, k), orc[k])
+    assert st.first_prime == orc["first"], ctx
+    assert st.last_prime == orc["last"], ctx
+    full = np.array(st.gap_hist_full, dtype=np.uint64)
+    assert np.array_equal(full, orc["hist"]), (ctx, np.nonzero(full != orc["hist"]))
+    assert st.twins == orc["hist"][1] and st.cousins == orc["hist"][2] and st.sexy == orc["hist"][3]
+    assert st.gap_hist[:201] == [int(x) for x in orc["hist"][:201]]
+    assert st.gap_hist[201] == int(orc["hist"][201:].sum())
+    assert st.large_gaps == int(orc["hist"][250:].sum())
+
+
+def test_golden_windows(vg, golden):
+    for w in golden["windows"]:
+        st = vg.range_stats(w["a"], w["b"], full=True)
+        assert st.count == w["count"], (w["a"], w["b"])
+        assert {str(k): v for k, v in sorted(st.gap_counts().items())} == w["gap_counts"]
+        for k in ("pi_4_1", "pi_4_3", "pi_3_1", "pi_3_2", "max_gap", "max_gap_start"):
+            assert getattr(st, k) == w[k], (w["a"], w["b"], k)
+        assert st.first_prime == w["first"] and st.last_prime == w["last"]
+
+
+def test_golden_context(vg, golden):
+    for c in golden["context"]:
+        N = c["N"]
+        with vg.Context(N) as ctx:
+            assert ctx.prime_count() == c["prime_count"], N
+            assert (ctx.twins(), ctx.cousin(), ctx.sexy()) == (c["twins"], c["cousin"], c["sexy"])
+            s = ctx.statistics()
+            r = c["stats"]
+            assert s.total_gaps == r["total"]
+            for mine, ref in ((s.mean_gap, r["mean"]), (s.std_dev, r["std"]),
+                              (s.skewness, r["skew"]), (s.kurtosis, r["kurt"])):
+                assert abs(mine - ref) <= 1e-9 * max(1.0, abs(ref)), N
+            cb = ctx.chebyshev()
+            if N >= 7:
+                assert (cb.pi_4_1, cb.pi_4_3) == (c["pi_4_1"], c["pi_4_3"]), N
+            else:   # the reference's Context leaves them 0 below 7 (context.cu:228-247)
+                assert (cb.pi_4_1, cb.pi_4_3) == (0, 0)
+
+
+@pytest.mark.parametrize("N,pi", [(2, 1), (3, 2), (5, 3), (10, 4), (100, 25), (10**6, 78498),
+                                  (10**7, 664579), (10**8, 5761455), (10**9, 50847534),
+                                  (10**10, 455052511)])
+def test_prime_count_known(vg, N, pi):
+    # test_primes.py:45-55, BASELINE pi(10^10)
+    assert vg.primes.prime_count(N) == pi
+
+
+def test_context_reference_values(vg, oracle_lib):
+    with vg.Context(10**9) as ctx:          # test_primes.py:162-188,438-443
+        assert (ctx.twins(), ctx.cousin(), ctx.sexy()) == (3424506, 3424679, 6089791)
+        assert ctx.large_gaps() == []
+        cb = ctx.chebyshev()
+        assert cb.difference == 551
+    with vg.Context(10**8) as ctx:
+        assert ctx.twins() == 440312
+        assert (ctx.chebyshev().pi_4_1, ctx.chebyshev().pi_4_3) == (2880504, 2880950)
+    with vg.Context(10**6) as ctx:
+        s = ctx.statistics()
+        assert s.total_gaps == 78497 and (ctx.twins(), ctx.cousin(), ctx.sexy()) == (8169, 8143, 13549)
+        assert (ctx.chebyshev().pi_4_1, ctx.chebyshev().pi_4_3) == (39175, 39322)
+    for N in (10**4, 10**6, 10**7, 12345678):
+        view = oracle_lib.context_view(N)
+        with vg.Context(N) as ctx:
+            s = ctx.statistics()
+            assert (s.mean_gap, s.std_dev, s.skewness, s.kurtosis) == (
+                view["stats"]["mean"], view["stats"]["std"], view["stats"]["skew"], view["stats"]["kurt"])
+
+
+def test_minimal_profile_counts(vg):
+    with vg.Context(10**8, profile="minimal") as ctx:
+        assert ctx.prime_count() == 5761455
+
+
+def test_random_windows_vs_oracle(vg, oracle_lib):
+    rng = random.Random(7)
+    cases = [(0, 1), (0, 2), (0, 7), (0, 8), (1, 60), (29, 31), (30, 31), (31, 32), (0, 30 * 196608 + 1),
+             (30 * 196608 - 5, 30 * 196608 + 5), (10**14 - 10**6, 10**14), (10**14, 10**14 + 10**6),
+             (10**14 + 10**10 - 10**5, 10**14 + 10**10 + 1), (2, 3), (3, 5), (5, 6)]
+    for _ in range(80):
+        a = rng.randrange(0, 10**13)
+        cases.append((a, a + rng.choice([1, 17, 1000, 10**5, 3 * 10**6, 10**7])))
+    for _ in range(40):
+        a = rng.randrange(0, 10**7)
+        cases.append((a, a + rng.randrange(0, 10**6)))
+    for a, b in cases:
+        st = vg.range_stats(a, b, full=True)
+        orc = oracle_lib.range_stats(a, b)
+        assert_range_equal(st, orc, (a, b))
+
+
+def test_full_range_1e10_vs_oracle(vg, oracle_lib):
+    st = vg.range_stats(0, 10**10, full=True)
+    assert_range_equal(st, oracle_lib.range_stats(0, 10**10), "1e10")
+
+
+def test_offset_1e12_split_merge_and_known_count(vg):
+    # pi(10^12 + 10^10) - pi(10^12) = 361840208 (two sympy primepi calls)
+    a, b = 10**12, 10**12 + 10**10
+    whole = vg.range_stats(a, b, full=True)
+    assert whole.count == 361840208
+    mid = a + 3 * 10**9 + 12345
+    left, right = vg.range_stats(a, mid, full=True), vg.range_stats(mid, b, full=True)
+    from voss_gb300.shard import merge
+    m = merge([left, right])
+    for k in ("count", "pi_4_1", "pi_4_3", "pi_3_1", "pi_3_2", "max_gap", "max_gap_start",
+              "first_prime", "last_prime", "num_gaps"):
+        assert getattr(m, k) == getattr(whole, k), k
+    assert m.gap_hist_full == whole.gap_hist_full
+
+
+def test_offset_1e14_subwindows_vs_oracle(vg, oracle_lib):
+    a = 10**14
+    for off in (0, 123456789, 5 * 10**8, 10**9 - 3 * 10**6):
+        st = vg.range_stats(a + off, a + off + 3 * 10**6, full=True)
+        assert_range_equal(st, oracle_lib.range_stats(a + off, a + off + 3 * 10**6), off)
+
+
+def test_batch_same_alone_and_in_mix(vg, oracle_lib):
+    rng = random.Random(11)
+    ranges = []
+    for _ in range(300):
+        a = int(10 ** rng.uniform(0, 13))
+        w = int(10 ** rng.uniform(0, 7))
+        ranges.append((a, a + w))
+    ranges += [(5, 5), (0, 0), (100, 50)]
+    res = vg.range_stats_batch(ranges)
+    for (a, b), r in zip(ranges, res):
+        alone = vg.range_stats(a, b)
+        assert r == alone, (a, b)
+    for (a, b), r in list(zip(ranges, res))[:60]:
+        orc = oracle_lib.range_stats(a, b)
+        assert r.count == orc["count"] and r.max_gap == orc["max_gap"], (a, b)
+
+
+def test_large_gaps_and_boundaries(vg, oracle_lib):
+    # gaps >= 500 exist in this window; position = second prime
+    a, b = 738832000000, 738834000000
+    with vg.Context(10**6) as ctx:
+        assert ctx.large_gaps() == []
+    st = vg.range_stats(a, b, full=True)
+    orc = oracle_lib.range_stats(a, b)
+    assert_range_equal(st, orc, "large")
+    assert st.max_gap == 540 and st.max_gap_start == 738832928467 - 540
+
+
+def test_progress_callback_chunks(vg):
+    seen = []
+    with vg.Context(10**6) as ctx:
+        ctx.set_progress(lambda *a: seen.append(a))
+        assert ctx.prime_count() == 78498
+    assert seen == [(1, 1, 78498 - 3, 78498)]
+    N = 120000000000       # three reference segments of 5*10^10+10
+    seen = []
+    with vg.Context(N, profile="minimal") as c1, vg.Context(N, profile="minimal") as c2:
+        c1.set_progress(lambda *a: seen.append(a))
+        assert c1.prime_count() == c2.prime_count()
+    assert [s[:2] for s in seen] == [(1, 3), (2, 3), (3, 3)]
+    assert seen[-1][3] == c2.prime_count() and sum(s[2] for s in seen) + 3 == seen[-1][3]
+
+
+def test_in_range(vg, oracle_lib):
+    p = vg.primes.in_range(10**9, 10**9 + 10**4)          # test_primes.py:235-240
+    assert len(p) == 487 and p[0] == 1000000007 and p[-1] == 1000009999
+    assert vg.primes.in_range(2, 10) == [2, 3, 5, 7]
+    assert vg.primes.in_range(10, 30) == [11, 13, 17, 19, 23, 29]
+    assert vg.primes.in_range(100, 130) == [101, 103, 107, 109, 113, 127]
+    assert vg.primes.in_range(20, 22) == [] and vg.primes.in_range(100, 100) == []
+    assert len(vg.primes.in_range(10, 100)) == 21
+    rng = random.Random(3)
+    for _ in range(20):
+        a = rng.randrange(0, 10**12)
+        b = a + rng.randrange(0, 10**6)
+        assert vg.primes.in_range_with_limit(a, b, 10**6) == oracle_lib.primes_in_range(a, b).tolist()
+    with pytest.raises(vg.VossError):
+        vg.primes.in_range_with_limit(0, 10**6, 1000)
+
+
+def test_sophie_germain(vg, oracle_lib):
+    for N, want in ((10, 3), (30, 6), (1000, 37)):       # test_primes.py:557-574
+        with vg.Context(N) as ctx:
+            assert ctx.sophie_germain() == want
+    N = 10**6 + 7
+    ps = oracle_lib.primes_in_range(0, 2 * N + 1)
+    s = set(ps.tolist())
+    want = sum(1 for p in ps if p <= N and 2 * p + 1 in s)
+    with vg.Context(N) as ctx:
+        assert ctx.sophie_germain() == want
+
+
+def test_goldbach_golden_and_oracle(vg, golden, oracle_lib):
+    g = golden["goldbach"]
+    r = vg.conjectures.goldbach_minp(g["N"])
+    assert r["minp"].tolist() == g["minp"] and r["max"] == g["max"]
+    for N in (4, 5, 6, 100, 65537 * 2, 10**7 + 1):
+        mine = vg.conjectures.goldbach_minp(N)
+        orc = oracle_lib.goldbach_minp(N)
+        assert np.array_equal(mine["minp"], orc["minp"]), N
+        assert mine["max"] == orc["max"] and mine["sum"] == orc["sum"], N
+        assert np.array_equal(mine["hist"], orc["hist"]), N
+        assert mine["counterexamples"] == 0
+    assert vg.conjectures.test_goldbach_upto(10**6)["status"] == "no_counterexample_found_upto_N"
+    assert list(vg.conjectures.iter_goldbach_upto(1000)) == []
+
+
+@pytest.mark.slow
+def test_goldbach_1e9_checksums(vg, oracle_lib):
+    mine = vg.conjectures.goldbach_minp(10**9, want_array=False)
+    orc = oracle_lib.goldbach_minp(10**9, want_array=False)
+    assert mine["max"] == orc["max"] and mine["sum"] == orc["sum"]
+    assert np.array_equal(mine["hist"], orc["hist"])
+    assert mine["counterexamples"] == 0
+
+
+def test_configs_agree(vg, oracle_lib):
+    """Segment size, CTA size and tier split change the schedule, not the result."""
+    base = vg.primes.get_config()
+    try:
+        cases = [(0, 3 * 10**8), (10**12, 10**12 + 10**8), (987654321, 987654321 + 5 * 10**7)]
+        want = [oracle_lib.range_stats(a, b) for a, b in cases]
+        for cfg in (dict(seg_bytes=65536, threads=512, tier_split=1024, auto_tune=0),
+                    dict(seg_bytes=196608, threads=1024, tier_split=4096, auto_tune=0),
+                    dict(seg_bytes=32768, threads=256, tier_split=37, auto_tune=0),
+                    dict(seg_bytes=131072, threads=768, tier_split=100000, ctas_per_sm=1, auto_tune=0)):
+            vg.primes.set_config(**cfg)
+            for (a, b), w in zip(cases, want):
+                assert_range_equal(vg.range_stats(a, b, full=True), w, (cfg, a, b))
+    finally:
+        vg.primes.set_config(**base)

@@ -1,0 +1,396 @@
+// engine.cpp -- host side of the GB300 sieve.
+//
+// Replaces the reference's per-call host orchestration
+// (library/src/primes/context.cu:212-559, prime_count.cu:141-293,
+// range.cu:99-262).  Differences by design:
+//   * the sieving-prime table (primes >= 37, with Barrett constants and the
+//     eight residue-class starts of each prime) is built once per process and
+//     stays resident on the device, growing on demand up to sqrt(10^14+10^10);
+//   * a run is two kernel launches for any number of ranges and segments,
+//     with no per-segment host work, no per-prime launches and no
+//     synchronisation until the results are read;
+//   * all buffers are reused across calls (grow-only).
+#include "engine.h"
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <numeric>
+
+#include "voss/voss.h"
+
+namespace vg {
+
+void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    int code = (e == cudaErrorMemoryAllocation) ? VOSS_ERR_OUT_OF_MEMORY
+             : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? VOSS_ERR_NO_CUDA
+             : VOSS_ERR_CUDA;
+    throw Error(code, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+uint64_t isqrt_u64(uint64_t x) {
+  uint64_t lo = 0, hi = 1ull << 32;
+  while (lo < hi) {
+    const uint64_t mid = lo + (hi - lo + 1) / 2;
+    if (mid <= x / mid) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+void DevBuf::reserve(size_t n) {
+  if (n <= bytes && ptr) return;
+  release();
+  size_t want = std::max<size_t>(n, 256);
+  check_cuda(cudaMalloc(&ptr, want), "cudaMalloc");
+  bytes = want;
+}
+
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+void HostPinned::reserve(size_t n) {
+  if (n <= bytes && ptr) return;
+  if (ptr) cudaFreeHost(ptr);
+  ptr = nullptr;
+  bytes = 0;
+  size_t want = std::max<size_t>(n, 256);
+  check_cuda(cudaMallocHost(&ptr, want), "cudaMallocHost");
+  bytes = want;
+}
+
+HostPinned::~HostPinned() {
+  if (ptr) cudaFreeHost(ptr);
+}
+
+static const uint32_t kW30[8] = {1, 7, 11, 13, 17, 19, 23, 29};
+// Largest segment any config may use; tiles are extended by this much.
+static const uint32_t kMaxSegBytes = 221184;
+
+static int64_t inverse_mod(int64_t a, int64_t m) {
+  int64_t t = 0, nt = 1, r = m, nr = a % m;
+  while (nr) {
+    const int64_t q = r / nr;
+    int64_t tmp = nt; nt = t - q * nt; t = tmp;
+    tmp = nr; nr = r - q * nr; r = tmp;
+  }
+  return t < 0 ? t + m : t;
+}
+
+Engine& Engine::for_current_device() {
+  static std::mutex reg_mu;
+  static std::vector<std::unique_ptr<Engine>> engines;
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> g(reg_mu);
+  if ((int)engines.size() <= dev) engines.resize(dev + 1);
+  if (!engines[dev]) {
+    std::unique_ptr<Engine> e(new Engine());
+    e->device = dev;
+    e->init();
+    engines[dev] = std::move(e);
+  }
+  return *engines[dev];
+}
+
+void Engine::init() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) throw Error(VOSS_ERR_NO_CUDA, "No CUDA device available");
+  cudaDeviceProp prop;
+  check_cuda(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+  sm_count = (uint32_t)prop.multiProcessorCount;
+  max_smem_optin = prop.sharedMemPerBlockOptin;
+  name = prop.name;
+  check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  // Fit the default segment into what this device offers.
+  while (sieve_smem_bytes(cfg.seg_bytes, cfg.threads) > max_smem_optin && cfg.seg_bytes > 16384)
+    cfg.seg_bytes -= 8192;
+  build_tiles();
+  scratch.eng = this;
+  scratch.device = device;
+  ensure_table(65536);
+}
+
+void Engine::build_tiles() {
+  auto make = [&](const uint32_t* ps, int nps, uint32_t period, DevBuf& dst) {
+    const size_t len = period + kMaxSegBytes + 64;
+    std::vector<uint8_t> t((len + 3) & ~size_t(3), 0);
+    for (uint32_t j = 0; j < period; ++j) {
+      uint8_t v = 0;
+      for (int o = 0; o < 8; ++o) {
+        const uint64_t x = 30ull * j + kW30[o];
+        bool comp = false;
+        for (int i = 0; i < nps; ++i) comp |= (x % ps[i]) == 0;
+        if (!comp) v |= (uint8_t)(1u << o);
+      }
+      t[j] = v;
+    }
+    for (size_t j = period; j < t.size(); ++j) t[j] = t[j - period];
+    dst.reserve(t.size());
+    check_cuda(cudaMemcpy(dst.ptr, t.data(), t.size(), cudaMemcpyHostToDevice), "tile upload");
+  };
+  const uint32_t a[4] = {7, 11, 13, 17};
+  const uint32_t b[4] = {19, 23, 29, 31};
+  make(a, 4, kTileAPeriod, tileA);
+  make(b, 4, kTileBPeriod, tileB);
+}
+
+void Engine::ensure_table(uint64_t pmax) {
+  if (pmax <= table_limit) return;
+  uint64_t lim = std::max<uint64_t>(pmax, std::min<uint64_t>(2 * table_limit, isqrt_u64(kMaxB) + 64));
+  lim = std::max<uint64_t>(lim, 4096);
+  // plain byte sieve of [0, lim]
+  std::vector<uint8_t> comp(lim + 1, 0);
+  for (uint64_t i = 2; i * i <= lim; ++i)
+    if (!comp[i])
+      for (uint64_t j = i * i; j <= lim; j += i) comp[j] = 1;
+  std::vector<uint32_t> P;
+  P.reserve(lim / 10 + 16);
+  for (uint64_t i = kFirstTablePrime; i <= lim; ++i)
+    if (!comp[i]) P.push_back((uint32_t)i);
+  const size_t n = P.size();
+  const size_t stride = (n + 31) & ~size_t(31);
+  std::vector<uint64_t> M(n);
+  std::vector<uint32_t> R(8 * stride, 0);
+  for (size_t i = 0; i < n; ++i) {
+    const uint64_t p = P[i];
+    M[i] = UINT64_MAX / p;
+    const uint64_t inv30 = (uint64_t)inverse_mod((int64_t)(30 % p), (int64_t)p);
+    for (int o = 0; o < 8; ++o)
+      R[o * stride + i] = (uint32_t)(((p - kW30[o] % p) % p) * inv30 % p);
+  }
+  // Plans launched earlier may still read the old table.
+  check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize(table)");
+  dP.reserve(std::max<size_t>(n, 1) * 4);
+  dM.reserve(std::max<size_t>(n, 1) * 8);
+  dR.reserve(std::max<size_t>(stride, 32) * 8 * 4);
+  if (n) {
+    check_cuda(cudaMemcpy(dP.ptr, P.data(), n * 4, cudaMemcpyHostToDevice), "table P");
+    check_cuda(cudaMemcpy(dM.ptr, M.data(), n * 8, cudaMemcpyHostToDevice), "table M");
+    check_cuda(cudaMemcpy(dR.ptr, R.data(), R.size() * 4, cudaMemcpyHostToDevice), "table R");
+  }
+  rstride = stride;
+  hP.swap(P);
+  table_limit = lim;
+}
+
+uint32_t Engine::primes_below_sq(uint64_t b) const {
+  if (b <= 1) return 0;
+  const uint64_t r = isqrt_u64(b - 1);     // p*p < b  <=>  p <= isqrt(b-1)
+  return (uint32_t)(std::upper_bound(hP.begin(), hP.end(), (uint64_t)std::min<uint64_t>(r, UINT32_MAX),
+                                     [](uint64_t v, uint32_t p) { return v < p; }) - hP.begin());
+}
+
+uint32_t Engine::index_of(uint32_t p) const {
+  return (uint32_t)(std::lower_bound(hP.begin(), hP.end(), p) - hP.begin());
+}
+
+Config Engine::tuned_for(uint64_t a, uint64_t b) const {
+  Config c = cfg;
+  if (!cfg.auto_tune) return c;
+  // Offset regimes: for small ranges a smaller segment spreads the work over
+  // more SMs; the split between warp-per-prime and thread-per-prime marking
+  // moves with the segment size (about S/96 clears per class at the split).
+  const uint64_t width = b > a ? b - a : 0;
+  const uint64_t bytes = width / 30 + 1;
+  uint32_t s = cfg.seg_bytes;
+  const uint64_t want_segs = (uint64_t)sm_count * cfg.ctas_per_sm;
+  while (s > 16384 && bytes / s < want_segs) s /= 2;
+  c.seg_bytes = (s + 127) & ~127u;
+  c.tier_split = std::max<uint32_t>(256, std::min<uint32_t>(cfg.tier_split, c.seg_bytes / 96));
+  return c;
+}
+
+// ---------------------------------------------------------------------------
+// Plan
+// ---------------------------------------------------------------------------
+void Plan::prepare(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl) {
+  Engine& E = *eng;
+  flags = fl;
+  nreq = n;
+  uint64_t max_b = 0, min_a = UINT64_MAX;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (b[i] > kMaxB) throw Error(VOSS_ERR_OUT_OF_RANGE, "range end exceeds 10^14 + 10^10 + 1");
+    if (b[i] > a[i]) { max_b = std::max(max_b, b[i]); min_a = std::min(min_a, a[i]); }
+  }
+  cfg = (n == 1 && max_b) ? E.tuned_for(a[0], b[0]) : E.cfg;
+  if (!E.cfg.auto_tune) cfg = E.cfg;
+  if (max_b > 1) E.ensure_table(isqrt_u64(max_b - 1));
+  tier_split_idx = E.index_of(cfg.tier_split);
+
+  host_reqs.assign(n, ReqDesc{});
+  uint64_t segs_total = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    ReqDesc& r = host_reqs[i];
+    r.a = a[i];
+    r.b = b[i];
+    r.seg_base = segs_total;
+    if (b[i] > a[i]) {
+      r.k_lo = a[i] / 30;
+      r.k_hi = (b[i] + 29) / 30;
+      r.nseg = (r.k_hi - r.k_lo + cfg.seg_bytes - 1) / cfg.seg_bytes;
+      r.nprimes = E.primes_below_sq(b[i]);
+    }
+    segs_total += r.nseg;
+  }
+  total_segs = segs_total;
+  if (flags & kFlagBitmap) {
+    if (n != 1) throw Error(VOSS_ERR_INTERNAL, "bitmap output needs exactly one range");
+    const uint64_t words = (host_reqs[0].k_hi - host_reqs[0].k_lo + 3) / 4 + 1;
+    bitmap.reserve(words * 4);
+  }
+  reqs.reserve(sizeof(ReqDesc) * std::max<uint32_t>(n, 1));
+  segs.reserve(sizeof(SegRec) * std::max<uint64_t>(total_segs, 1));
+  acc.reserve(sizeof(ReqAccum) * std::max<uint32_t>(n, 1));
+  results.reserve(sizeof(ReqResult) * std::max<uint32_t>(n, 1));
+  large.reserve(sizeof(LargeGapRec) * large_cap);
+  nlarge.reserve(sizeof(unsigned int));
+  if (n)
+    check_cuda(cudaMemcpyAsync(reqs.ptr, host_reqs.data(), sizeof(ReqDesc) * n,
+                               cudaMemcpyHostToDevice, E.stream), "upload requests");
+  check_cuda(cudaStreamSynchronize(E.stream), "cudaStreamSynchronize(prepare)");
+  const uint64_t cap = (uint64_t)E.sm_count * cfg.ctas_per_sm;
+  grid = (uint32_t)std::min<uint64_t>(total_segs, cap);
+}
+
+Plan::~Plan() {
+  for (cudaEvent_t& e : ev)
+    if (e) cudaEventDestroy(e);
+}
+
+void Plan::kernel_ms(float* sieve_ms, float* finalize_ms) {
+  if (!ev[2]) throw Error(VOSS_ERR_INVALID_ARG, "plan has not been launched");
+  check_cuda(cudaEventSynchronize(ev[2]), "plan events");
+  if (sieve_ms) check_cuda(cudaEventElapsedTime(sieve_ms, ev[0], ev[1]), "event time");
+  if (finalize_ms) check_cuda(cudaEventElapsedTime(finalize_ms, ev[1], ev[2]), "event time");
+}
+
+void Plan::launch(cudaStream_t s) {
+  Engine& E = *eng;
+  for (cudaEvent_t& e : ev)
+    if (!e) check_cuda(cudaEventCreate(&e), "cudaEventCreate");
+  prm.reqs = reqs.as<ReqDesc>();
+  prm.nreq = nreq;
+  prm.total_segs = total_segs;
+  prm.P = E.dP.as<uint32_t>();
+  prm.M = E.dM.as<uint64_t>();
+  prm.R = E.dR.as<uint32_t>();
+  prm.rstride = E.rstride;
+  prm.tileA = E.tileA.as<uint32_t>();
+  prm.tileB = E.tileB.as<uint32_t>();
+  prm.seg_bytes = cfg.seg_bytes;
+  prm.tier_split = tier_split_idx;
+  prm.segs = segs.as<SegRec>();
+  prm.acc = acc.as<ReqAccum>();
+  prm.large = large.as<LargeGapRec>();
+  prm.n_large = nlarge.as<unsigned int>();
+  prm.large_cap = large_cap;
+  prm.flags = flags;
+  prm.bitmap = bitmap.as<uint32_t>();
+  if (nreq == 0) return;
+  check_cuda(cudaMemsetAsync(acc.ptr, 0, sizeof(ReqAccum) * nreq, s), "memset accumulators");
+  check_cuda(cudaMemsetAsync(nlarge.ptr, 0, sizeof(unsigned int), s), "memset large count");
+  check_cuda(cudaEventRecord(ev[0], s), "event");
+  check_cuda(launch_sieve(prm, grid, cfg.threads, s), "sieve_segments_kernel");
+  check_cuda(cudaEventRecord(ev[1], s), "event");
+  check_cuda(launch_finalize(reqs.as<ReqDesc>(), segs.as<SegRec>(), acc.as<ReqAccum>(),
+                             large.as<LargeGapRec>(), nlarge.as<unsigned int>(), large_cap,
+                             results.as<ReqResult>(), nreq, s),
+             "finalize_kernel");
+  check_cuda(cudaEventRecord(ev[2], s), "event");
+}
+
+const ReqResult* Plan::fetch(cudaStream_t s) {
+  host_results.reserve(sizeof(ReqResult) * std::max<uint32_t>(nreq, 1));
+  if (nreq)
+    check_cuda(cudaMemcpyAsync(host_results.ptr, results.ptr, sizeof(ReqResult) * nreq,
+                               cudaMemcpyDeviceToHost, s), "download results");
+  check_cuda(cudaStreamSynchronize(s), "sieve run");
+  return static_cast<const ReqResult*>(host_results.ptr);
+}
+
+std::vector<LargeGapRec> Plan::fetch_large(cudaStream_t s) {
+  unsigned int n = 0;
+  check_cuda(cudaMemcpyAsync(&n, nlarge.ptr, sizeof(n), cudaMemcpyDeviceToHost, s), "large count");
+  check_cuda(cudaStreamSynchronize(s), "large count");
+  if (n > large_cap)
+    throw Error(VOSS_ERR_INTERNAL, "large-gap buffer overflow (" + std::to_string(n) + " gaps)");
+  std::vector<LargeGapRec> v(n);
+  if (n) {
+    check_cuda(cudaMemcpyAsync(v.data(), large.ptr, sizeof(LargeGapRec) * n,
+                               cudaMemcpyDeviceToHost, s), "large gaps");
+    check_cuda(cudaStreamSynchronize(s), "large gaps");
+  }
+  return v;
+}
+
+uint64_t Plan::wheel_bytes() const {
+  uint64_t t = 0;
+  for (const ReqDesc& r : host_reqs) t += r.k_hi - r.k_lo;
+  return t;
+}
+
+uint64_t Plan::algorithmic_clears() const {
+  // Exactly the clears the marking tiers perform: for each table prime p
+  // (>= 37, p*p < b) and class o, the k in [k_lo, k_hi) with
+  // k = R (mod p) and 30k + W30[o] >= p*p.
+  const Engine& E = *eng;
+  uint64_t total = 0;
+  for (const ReqDesc& r : host_reqs) {
+    for (uint32_t i = 0; i < r.nprimes; ++i) {
+      const uint64_t p = E.hP[i];
+      const int64_t inv30 = inverse_mod((int64_t)(30 % p), (int64_t)p);
+      for (int o = 0; o < 8; ++o) {
+        const uint64_t rr = ((p - kW30[o] % p) % p) * (uint64_t)inv30 % p;
+        uint64_t k = r.k_lo + (rr + p - r.k_lo % p) % p;
+        const uint64_t n = 30 * k + kW30[o];
+        if (n < p * p) k += ((p * p - n + 30 * p - 1) / (30 * p)) * p;
+        if (k < r.k_hi) total += (r.k_hi - 1 - k) / p + 1;
+      }
+    }
+  }
+  return total;
+}
+
+const ReqResult* Engine::run(uint32_t n, const uint64_t* a, const uint64_t* b,
+                             std::vector<LargeGapRec>* lg) {
+  scratch.prepare(n, a, b, 0);
+  scratch.launch(stream);
+  const ReqResult* r = scratch.fetch(stream);
+  if (lg) *lg = scratch.fetch_large(stream);
+  return r;
+}
+
+void to_public(const ReqResult& r, uint64_t a, uint64_t b, voss_range_stats_t* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->a = a;
+  o->b = b;
+  o->count = r.count;
+  o->twins = r.hist[1];
+  o->cousins = r.hist[2];
+  o->sexy = r.hist[3];
+  o->pi_4_1 = r.c41;
+  o->pi_4_3 = r.c43;
+  o->pi_3_1 = r.c31;
+  o->pi_3_2 = r.c32;
+  o->first_prime = r.first;
+  o->last_prime = r.last;
+  o->max_gap = r.max_gap;
+  o->max_gap_start = r.max_gap_start;
+  o->num_gaps = r.num_gaps;
+  uint64_t over = 0, large = 0;
+  for (int i = 0; i < kHistBins; ++i) {
+    if (i < VOSS_GAP_BINS - 1) o->gap_hist[i] = r.hist[i];
+    else over += r.hist[i];
+    if (i >= (int)(kLargeGap / 2)) large += r.hist[i];
+  }
+  o->gap_hist[VOSS_GAP_BINS - 1] = over;
+  o->large_gaps = large;
+}
+
+}  // namespace vg

@@ -1,0 +1,149 @@
+// engine.h -- host side of the GB300 sieve: resident prime table, presieve
+// tiles, launch plans.  Internal C++ (throws vg::Error); the C ABI in
+// capi.cpp turns errors into VOSS_* codes.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "sieve.cuh"
+#include "voss/voss_gb300.h"
+
+namespace vg {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void check_cuda(cudaError_t e, const char* what);
+
+// Largest b (exclusive) a range may end at: 10^14 + 10^10 + 1.
+constexpr uint64_t kMaxB = 100000000000000ull + 10000000000ull + 1ull;
+
+uint64_t isqrt_u64(uint64_t x);
+
+// Device buffer that only grows.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  void reserve(size_t n);
+  void release();
+  template <class T> T* as() const { return static_cast<T*>(ptr); }
+  ~DevBuf() { release(); }
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+};
+
+struct HostPinned {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  void reserve(size_t n);
+  ~HostPinned();
+  HostPinned() = default;
+  HostPinned(const HostPinned&) = delete;
+  HostPinned& operator=(const HostPinned&) = delete;
+};
+
+struct Config {
+  uint32_t seg_bytes = 196608;
+  uint32_t threads = 1024;
+  uint32_t tier_split = 2048;
+  uint32_t ctas_per_sm = 1;
+  uint32_t auto_tune = 1;
+};
+
+class Engine;
+
+// A prepared batch of ranges with its device buffers.
+struct Plan {
+  Engine* eng = nullptr;
+  uint32_t nreq = 0;
+  uint64_t total_segs = 0;
+  uint32_t grid = 0;
+  Config cfg;
+  uint32_t tier_split_idx = 0;
+  std::vector<ReqDesc> host_reqs;
+  DevBuf reqs, segs, acc, large, nlarge, results, bitmap;
+  HostPinned host_results;
+  uint32_t large_cap = 1u << 16;
+  uint32_t flags = 0;
+  SieveParams prm{};
+  int device = 0;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // before sieve, after sieve, after finalize
+
+  ~Plan();
+  Plan() = default;
+  Plan(const Plan&) = delete;
+  Plan& operator=(const Plan&) = delete;
+
+  // Kernels per run (sieve + finalize).
+  static constexpr uint32_t kKernels = 2;
+
+  void prepare(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t flags);
+  void launch(cudaStream_t s);
+  // Copy results of the last run to host memory owned by the plan.
+  const ReqResult* fetch(cudaStream_t s);
+  std::vector<LargeGapRec> fetch_large(cudaStream_t s);
+  uint64_t algorithmic_clears() const;
+  uint64_t wheel_bytes() const;
+  // Durations of the sieve and finalize kernels of the last launch (CUDA
+  // events recorded on the launching stream).
+  void kernel_ms(float* sieve_ms, float* finalize_ms);
+};
+
+class Engine {
+ public:
+  static Engine& for_current_device();
+
+  std::mutex mu;     // one caller at a time per device
+  int device = 0;
+  uint32_t sm_count = 0;
+  size_t max_smem_optin = 0;
+  std::string name;
+  cudaStream_t stream = nullptr;
+  Config cfg;
+
+  // Resident sieving-prime table: primes >= 37 up to table_limit.
+  std::vector<uint32_t> hP;
+  uint64_t table_limit = 0;
+  DevBuf dP, dM, dR;
+  uint64_t rstride = 0;
+  DevBuf tileA, tileB;
+
+  // Scratch plan reused by the synchronous entry points.
+  Plan scratch;
+
+  void ensure_table(uint64_t pmax);
+  uint32_t primes_below_sq(uint64_t b) const;   // table primes p with p*p < b
+  uint32_t index_of(uint32_t p) const;           // first table index with P >= p
+  Config tuned_for(uint64_t a, uint64_t b) const;
+
+  // Run ranges synchronously on the engine stream.
+  const ReqResult* run(uint32_t n, const uint64_t* a, const uint64_t* b,
+                       std::vector<LargeGapRec>* large = nullptr);
+
+ private:
+  Engine() = default;
+  void init();
+  void build_tiles();
+};
+
+void smem_peaks(Engine& E, double* ldst_gbs, double* atomic_gbs);
+
+void to_public(const ReqResult& r, uint64_t a, uint64_t b, voss_range_stats_t* out);
+
+// Launchers defined in sieve.cu.
+size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads);
+cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads,
+                         cudaStream_t stream);
+cudaError_t launch_finalize(const ReqDesc* reqs, const SegRec* segs, ReqAccum* acc,
+                            LargeGapRec* large, unsigned int* n_large, uint32_t large_cap,
+                            ReqResult* out, uint32_t nreq, cudaStream_t stream);
+
+}  // namespace vg

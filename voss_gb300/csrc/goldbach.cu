@@ -1,0 +1,471 @@
+// goldbach.cu -- kernels that read a sieved wheel bitmap.
+//
+//  * goldbach_minp_kernel: for every even n in [6, N] the smallest odd prime
+//    p with n - p prime.  The reference walks the prime list per n and stops
+//    at the first p whose partner is set in a 64-bit-per-64-numbers bitmap
+//    (goldbach_upto.cu:25-46); it keeps only the counterexamples.  Here one
+//    CTA holds 32768 even n as a bit set U of unresolved n; for p = 3, 5, 7...
+//    the partners n - p of the whole tile are one shifted window of an
+//    odd-number bitmap, so U & window resolves 32 n per word operation.  The
+//    smallest p per n, its maximum and its histogram come out; the
+//    counterexamples are the n left in U once p > n/2.
+//  * sophie_germain_kernel: p <= N with 2p+1 prime (sophie_germain_upto.cu:
+//    22-33), read straight from the wheel bitmap: only p = 11, 23, 29 mod 30
+//    can qualify, and their 2p+1 falls on fixed bits of byte 2k or 2k+1.
+//  * extract kernels: the sorted prime list of a range (range.cu:225-259),
+//    by per-block popcount, an exclusive scan, and an ordered write.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "goldbach.h"
+#include "voss/voss.h"
+
+namespace vg {
+
+namespace {
+
+__constant__ uint8_t kClassOf[30] = {
+    0xFF, 0, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 1, 0xFF, 0xFF, 0xFF, 2, 0xFF, 3, 0xFF,
+    0xFF, 0xFF, 4, 0xFF, 5, 0xFF, 0xFF, 0xFF, 6, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 7};
+
+__device__ __forceinline__ uint64_t umin64(uint64_t x, uint64_t y) { return x < y ? x : y; }
+
+__device__ __forceinline__ uint32_t wheel_bit(const uint32_t* __restrict__ wb, uint64_t k,
+                                              uint32_t o) {
+  return (__ldg(wb + (k >> 2)) >> ((uint32_t)((k & 3) << 3) + o)) & 1u;
+}
+
+// Odd-number bitmap: bit i of `odd` <-> 2i+1, for 2i+1 <= limit.
+__global__ void odd_bitmap_kernel(const uint32_t* __restrict__ wb, uint32_t* __restrict__ odd,
+                                  uint64_t odd_words, uint64_t limit) {
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < odd_words;
+       w += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t m0 = 64 * w + 1;
+    uint64_t k = m0 / 30;
+    uint32_t r = (uint32_t)(m0 - 30 * k);
+    uint32_t out = 0;
+    for (uint32_t j = 0; j < 32; ++j) {
+      const uint64_t m = m0 + 2 * j;
+      if (m > limit) break;
+      const uint32_t c = kClassOf[r];
+      uint32_t bit;
+      if (c != 0xFF) bit = wheel_bit(wb, k, c);
+      else bit = (m == 3 || m == 5);
+      out |= bit << j;
+      r += 2;
+      if (r >= 30) { r -= 30; ++k; }
+    }
+    odd[w] = out;
+  }
+}
+
+constexpr int kGbThreads = 256;
+constexpr int kGbWords = 4;                                  // U words per thread
+constexpr uint32_t kGbTile = kGbThreads * kGbWords * 32;     // even n per tile
+constexpr uint32_t kGbSmemHist = 4096;                       // p < 4096 counted in smem
+constexpr size_t kGbSmemBytes = kGbSmemHist * 4 + kGbTile * 2;
+
+struct GbOut {
+  uint32_t* minp;                    // optional, index (n-4)/2
+  unsigned long long* hist;          // by p
+  unsigned int* max_minp;
+  unsigned long long* sum_minp;
+  unsigned long long* n_ce;
+  unsigned long long* ce;
+  uint64_t ce_cap;
+  unsigned long long* probes;
+  unsigned int* err;                 // 1: the prime list ran out before n/2
+};
+
+__global__ void __launch_bounds__(kGbThreads, 2)
+goldbach_minp_kernel(const uint32_t* __restrict__ odd, uint64_t odd_words,
+                     const uint32_t* __restrict__ oddp, uint32_t noddp, uint64_t N,
+                     uint64_t ntiles, GbOut out) {
+  extern __shared__ __align__(16) uint32_t gb_smem[];
+  uint32_t* shist = gb_smem;                                          // kGbSmemHist
+  uint16_t* sminp = reinterpret_cast<uint16_t*>(gb_smem + kGbSmemHist);  // kGbTile
+  const uint32_t tid = threadIdx.x;
+  const uint64_t n_last = N & ~1ull;           // largest even n
+  uint32_t lmax = 0;
+  unsigned long long lsum = 0, lprobes = 0;
+  for (uint32_t i = tid; i < kGbSmemHist; i += kGbThreads) shist[i] = 0;
+
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint64_t n0 = 6 + tile * 2ull * kGbTile;
+    const uint64_t nmax = umin64(n_last, n0 + 2ull * (kGbTile - 1));
+    const uint32_t tcount = (uint32_t)((nmax - n0) / 2 + 1);
+    for (uint32_t i = tid; i < kGbTile; i += kGbThreads) sminp[i] = 0;
+    uint32_t U[kGbWords];
+#pragma unroll
+    for (int q = 0; q < kGbWords; ++q) {
+      const uint32_t t0 = 32u * (tid * kGbWords + q);
+      U[q] = t0 >= tcount ? 0u : (tcount - t0 >= 32 ? 0xFFFFFFFFu : ((1u << (tcount - t0)) - 1u));
+    }
+    __syncthreads();
+    bool exhausted = true;
+    for (uint32_t pi = 0; pi < noddp; ++pi) {
+      const uint32_t p = __ldg(oddp + pi);
+      if (2ull * p > nmax) { exhausted = false; break; }
+      if ((pi & 7u) == 0) {
+        if (!__syncthreads_or((U[0] | U[1] | U[2] | U[3]) != 0)) { exhausted = false; break; }
+      }
+      const int64_t base = ((int64_t)n0 - (int64_t)p - 1) / 2;   // odd-bit index at t = 0
+#pragma unroll
+      for (int q = 0; q < kGbWords; ++q) {
+        if (!U[q]) continue;
+        const uint32_t w = tid * kGbWords + q;
+        const int64_t bi = base + 32ll * w;
+        const int64_t wi = bi >> 5;                               // floor
+        const uint32_t sh = (uint32_t)(bi & 31);
+        const uint32_t lo = (wi >= 0 && (uint64_t)wi < odd_words) ? __ldg(odd + wi) : 0u;
+        const uint32_t hi = (wi + 1 >= 0 && (uint64_t)(wi + 1) < odd_words) ? __ldg(odd + wi + 1) : 0u;
+        const uint32_t win = __funnelshift_r(lo, hi, sh);
+        uint32_t hit = U[q] & win;
+        ++lprobes;
+        if (hit) {
+          U[q] &= ~hit;
+          do {
+            const uint32_t j = (uint32_t)__ffs(hit) - 1u;
+            hit &= hit - 1u;
+            sminp[32u * w + j] = (uint16_t)p;
+          } while (hit);
+        }
+      }
+    }
+    // Whatever is left: counterexamples, unless the prime list ran out first.
+#pragma unroll
+    for (int q = 0; q < kGbWords; ++q) {
+      uint32_t u = U[q];
+      if (!u) continue;
+      if (exhausted) { atomicOr(out.err, 1u); continue; }
+      while (u) {
+        const uint32_t j = (uint32_t)__ffs(u) - 1u;
+        u &= u - 1u;
+        const uint64_t n = n0 + 2ull * (32u * (tid * kGbWords + q) + j);
+        const unsigned long long slot = atomicAdd(out.n_ce, 1ull);
+        if (slot < out.ce_cap) out.ce[slot] = n;
+      }
+    }
+    __syncthreads();
+    const uint64_t obase = 1 + tile * (uint64_t)kGbTile;     // (n0 - 4) / 2
+    for (uint32_t i = tid; i < tcount; i += kGbThreads) {
+      const uint32_t p = sminp[i];
+      if (out.minp) out.minp[obase + i] = p;
+      lmax = max(lmax, p);
+      lsum += p;
+      if (p < kGbSmemHist) atomicAdd(&shist[p], 1u);
+      else atomicAdd(&out.hist[p], 1ull);
+    }
+    __syncthreads();
+  }
+  for (uint32_t i = tid; i < kGbSmemHist; i += kGbThreads)
+    if (shist[i]) atomicAdd(&out.hist[i], (unsigned long long)shist[i]);
+  // counterexamples contributed p = 0 to hist[0]; harmless, the host ignores bin 0
+  lmax = __reduce_max_sync(0xFFFFFFFFu, lmax);
+  if ((tid & 31) == 0) atomicMax(out.max_minp, lmax);
+  atomicAdd(out.sum_minp, lsum);
+  atomicAdd(out.probes, lprobes);
+}
+
+__global__ void sophie_germain_kernel(const uint32_t* __restrict__ wb, uint64_t N,
+                                      unsigned long long* __restrict__ count) {
+  // bytes k with 30k + 11 <= N
+  const uint64_t kmax = N >= 11 ? (N - 11) / 30 : 0;
+  unsigned long long c = 0;
+  if (N >= 11) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k <= kmax;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+      const uint64_t base = 30 * k;
+      if (wheel_bit(wb, k, 2) && wheel_bit(wb, 2 * k, 6)) ++c;                         // 11 -> 23
+      if (base + 23 <= N && wheel_bit(wb, k, 6) && wheel_bit(wb, 2 * k + 1, 4)) ++c;  // 23 -> 47
+      if (base + 29 <= N && wheel_bit(wb, k, 7) && wheel_bit(wb, 2 * k + 1, 7)) ++c;  // 29 -> 59
+    }
+  }
+  c = __reduce_add_sync(0xFFFFFFFFu, (unsigned)c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+constexpr int kExThreads = 512;
+constexpr int kExWords = 8;
+constexpr uint32_t kExBlockWords = kExThreads * kExWords;
+
+__global__ void extract_count_kernel(const uint32_t* __restrict__ wb, uint64_t nwords,
+                                     uint32_t* __restrict__ block_counts) {
+  const uint64_t w0 = blockIdx.x * (uint64_t)kExBlockWords + threadIdx.x * (uint64_t)kExWords;
+  uint32_t c = 0;
+#pragma unroll
+  for (int i = 0; i < kExWords; ++i)
+    if (w0 + i < nwords) c += __popc(wb[w0 + i]);
+  c = __reduce_add_sync(0xFFFFFFFFu, c);
+  __shared__ uint32_t s[kExThreads / 32];
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int i = 0; i < kExThreads / 32; ++i) t += s[i];
+    block_counts[blockIdx.x] = t;
+  }
+}
+
+__global__ void extract_write_kernel(const uint32_t* __restrict__ wb, uint64_t nwords,
+                                     uint64_t k_lo, const uint64_t* __restrict__ block_offsets,
+                                     uint64_t* __restrict__ out) {
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint64_t w0 = blockIdx.x * (uint64_t)kExBlockWords + tid * (uint64_t)kExWords;
+  uint32_t words[kExWords];
+  uint32_t c = 0;
+#pragma unroll
+  for (int i = 0; i < kExWords; ++i) {
+    words[i] = (w0 + i < nwords) ? wb[w0 + i] : 0u;
+    c += __popc(words[i]);
+  }
+  // block exclusive scan of c
+  uint32_t incl = c;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+    if ((int)lane >= d) incl += t;
+  }
+  __shared__ uint32_t s[kExThreads / 32];
+  if (lane == 31) s[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t v = lane < kExThreads / 32 ? s[lane] : 0u;
+    uint32_t iv = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, iv, d);
+      if ((int)lane >= d) iv += t;
+    }
+    if (lane < kExThreads / 32) s[lane] = iv - v;
+  }
+  __syncthreads();
+  uint64_t pos = block_offsets[blockIdx.x] + s[warp] + (incl - c);
+#pragma unroll
+  for (int i = 0; i < kExWords; ++i) {
+    uint32_t w = words[i];
+    const uint64_t kb = k_lo + 4 * (w0 + i);
+    while (w) {
+      const uint32_t b = (uint32_t)__ffs(w) - 1u;
+      w &= w - 1u;
+      out[pos++] = 30 * (kb + (b >> 3)) + (uint32_t)((kW30Packed >> ((b & 7u) << 3)) & 0xFFu);
+    }
+  }
+}
+
+// Sieve [0, limit] (or [a, b]) into a wheel bitmap on the device.
+const uint32_t* sieve_bitmap(Engine& E, Plan& plan, uint64_t a, uint64_t b_excl, uint64_t* nwords) {
+  plan.eng = &E;
+  plan.device = E.device;
+  plan.prepare(1, &a, &b_excl, kFlagBitmap);
+  plan.launch(E.stream);
+  *nwords = (plan.host_reqs[0].k_hi - plan.host_reqs[0].k_lo + 3) / 4;
+  return plan.bitmap.as<uint32_t>();
+}
+
+std::vector<uint32_t> odd_primes_below(uint32_t limit) {
+  std::vector<uint8_t> comp(limit + 1, 0);
+  std::vector<uint32_t> v;
+  for (uint32_t i = 2; i <= limit; ++i) {
+    if (comp[i]) continue;
+    if (i > 2) v.push_back(i);
+    for (uint64_t j = (uint64_t)i * i; j <= limit; j += i) comp[j] = 1;
+  }
+  return v;
+}
+
+}  // namespace
+
+struct GoldbachPlan {
+  Engine* eng = nullptr;
+  uint64_t N = 0;
+  Plan sieve;
+  DevBuf odd, oddp, minp, hist, scalars, ce;
+  uint64_t odd_words = 0, ntiles = 0, ce_cap = 0;
+  uint32_t grid = 0;
+  bool want_minp = false;
+};
+
+GoldbachPlan* goldbach_plan_create(Engine& E, uint64_t N) {
+  std::unique_ptr<GoldbachPlan> g(new GoldbachPlan());
+  g->eng = &E;
+  g->N = N;
+  const std::vector<uint32_t> op = odd_primes_below(65535);
+  g->oddp.reserve(op.size() * 4);
+  check_cuda(cudaMemcpy(g->oddp.ptr, op.data(), op.size() * 4, cudaMemcpyHostToDevice), "odd primes");
+  g->odd_words = (N / 2 + 1 + 31) / 32 + 2;
+  g->odd.reserve(g->odd_words * 4);
+  g->hist.reserve(sizeof(unsigned long long) * kGoldbachHistBins);
+  g->scalars.reserve(64);
+  g->ce_cap = 1024;
+  g->ce.reserve(8 * g->ce_cap);
+  g->ntiles = N >= 6 ? ((N & ~1ull) - 6) / (2ull * kGbTile) + 1 : 0;
+  g->grid = (uint32_t)std::min<uint64_t>(g->ntiles, (uint64_t)E.sm_count * 2);
+  g->sieve.eng = &E;
+  return g.release();
+}
+
+void goldbach_plan_launch(GoldbachPlan* g, cudaStream_t s) {
+  Engine& E = *g->eng;
+  // wheel bitmap of [0, N] (sieve kernel on the same stream)
+  {
+    uint64_t a = 0, b = g->N + 1;
+    if (!g->sieve.nreq || g->sieve.host_reqs[0].b != b) g->sieve.prepare(1, &a, &b, kFlagBitmap);
+    g->sieve.launch(s);
+  }
+  const uint32_t* wb = g->sieve.bitmap.as<uint32_t>();
+  odd_bitmap_kernel<<<E.sm_count * 8, 256, 0, s>>>(wb, g->odd.as<uint32_t>(), g->odd_words - 2, g->N);
+  check_cuda(cudaGetLastError(), "odd_bitmap_kernel");
+  check_cuda(cudaMemsetAsync(g->odd.as<uint32_t>() + (g->odd_words - 2), 0, 8, s), "odd pad");
+  check_cuda(cudaMemsetAsync(g->hist.ptr, 0, sizeof(unsigned long long) * kGoldbachHistBins, s), "hist");
+  check_cuda(cudaMemsetAsync(g->scalars.ptr, 0, 64, s), "scalars");
+  if (!g->ntiles) return;
+  auto* sc = g->scalars.as<unsigned long long>();
+  GbOut o;
+  o.minp = g->want_minp ? g->minp.as<uint32_t>() : nullptr;
+  o.hist = g->hist.as<unsigned long long>();
+  o.max_minp = reinterpret_cast<unsigned int*>(sc + 0);
+  o.sum_minp = sc + 1;
+  o.n_ce = sc + 2;
+  o.probes = sc + 3;
+  o.err = reinterpret_cast<unsigned int*>(sc + 4);
+  o.ce = g->ce.as<unsigned long long>();
+  o.ce_cap = g->ce_cap;
+  static bool attr_set = false;
+  if (!attr_set) {
+    check_cuda(cudaFuncSetAttribute(goldbach_minp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kGbSmemBytes), "goldbach smem");
+    attr_set = true;
+  }
+  goldbach_minp_kernel<<<g->grid, kGbThreads, kGbSmemBytes, s>>>(g->odd.as<uint32_t>(), g->odd_words,
+                                                      g->oddp.as<uint32_t>(), kGoldbachPrimes,
+                                                      g->N, g->ntiles, o);
+  check_cuda(cudaGetLastError(), "goldbach_minp_kernel");
+}
+
+void goldbach_plan_fetch(GoldbachPlan* g, GoldbachResult* r, cudaStream_t s) {
+  unsigned long long sc[5] = {0, 0, 0, 0, 0};
+  r->hist.assign(kGoldbachHistBins, 0);
+  check_cuda(cudaMemcpyAsync(sc, g->scalars.ptr, sizeof(sc), cudaMemcpyDeviceToHost, s), "scalars");
+  check_cuda(cudaMemcpyAsync(r->hist.data(), g->hist.ptr, 8ull * kGoldbachHistBins,
+                             cudaMemcpyDeviceToHost, s), "hist");
+  check_cuda(cudaStreamSynchronize(s), "goldbach run");
+  if (sc[4]) throw Error(VOSS_ERR_INTERNAL, "Goldbach: no prime below 65536 resolved some n");
+  const uint64_t nce = sc[2];
+  r->n_counterexamples = nce;
+  const uint64_t keep = std::min<uint64_t>(nce, g->ce_cap);
+  std::vector<uint64_t> ce(keep);
+  if (keep) {
+    check_cuda(cudaMemcpy(ce.data(), g->ce.ptr, 8 * keep, cudaMemcpyDeviceToHost), "ce");
+    std::sort(ce.begin(), ce.end());
+  }
+  r->counterexamples = ce;
+  r->hist[0] = 0;
+  // n = 4 = 2 + 2 is outside the kernel's tiles
+  r->max_minp = std::max<uint32_t>((uint32_t)sc[0], g->N >= 4 ? 2u : 0u);
+  r->sum_minp = sc[1] + (g->N >= 4 ? 2 : 0);
+  if (g->N >= 4) r->hist[2] += 1;
+}
+
+uint64_t goldbach_plan_probes(GoldbachPlan* g) {
+  unsigned long long sc[5];
+  check_cuda(cudaMemcpy(sc, g->scalars.ptr, sizeof(sc), cudaMemcpyDeviceToHost), "probes");
+  return sc[3];
+}
+
+void goldbach_plan_free(GoldbachPlan* g) { delete g; }
+
+GoldbachResult goldbach_run(Engine& E, uint64_t N, uint32_t* minp_host, uint64_t max_ce,
+                            float* kernel_ms) {
+  std::unique_ptr<GoldbachPlan> g(goldbach_plan_create(E, N));
+  const uint64_t nn = (N - 4) / 2 + 1;
+  if (minp_host) {
+    g->want_minp = true;
+    g->minp.reserve(4 * nn);
+  }
+  g->ce_cap = std::max<uint64_t>(std::min<uint64_t>(max_ce, 1ull << 24), 1);
+  g->ce.reserve(8 * g->ce_cap);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (kernel_ms) {
+    check_cuda(cudaEventCreate(&e0), "event");
+    check_cuda(cudaEventCreate(&e1), "event");
+    check_cuda(cudaEventRecord(e0, E.stream), "event");
+  }
+  goldbach_plan_launch(g.get(), E.stream);
+  if (kernel_ms) check_cuda(cudaEventRecord(e1, E.stream), "event");
+  GoldbachResult r;
+  goldbach_plan_fetch(g.get(), &r, E.stream);
+  if (kernel_ms) {
+    check_cuda(cudaEventElapsedTime(kernel_ms, e0, e1), "event");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  if (minp_host) {
+    check_cuda(cudaMemcpy(minp_host, g->minp.ptr, 4 * nn, cudaMemcpyDeviceToHost), "minp");
+    minp_host[0] = 2;  // n = 4
+  }
+  if (r.counterexamples.size() > max_ce) r.counterexamples.resize(max_ce);
+  return r;
+}
+
+uint64_t sophie_germain_count(Engine& E, uint64_t N) {
+  uint64_t seeds = (N >= 2) + (N >= 3) + (N >= 5);
+  if (N < 11) return seeds;
+  Plan plan;
+  uint64_t nw = 0;
+  const uint32_t* wb = sieve_bitmap(E, plan, 0, 2 * N + 2, &nw);
+  DevBuf cnt;
+  cnt.reserve(8);
+  check_cuda(cudaMemsetAsync(cnt.ptr, 0, 8, E.stream), "memset");
+  sophie_germain_kernel<<<E.sm_count * 8, 256, 0, E.stream>>>(wb, N, cnt.as<unsigned long long>());
+  check_cuda(cudaGetLastError(), "sophie_germain_kernel");
+  unsigned long long c = 0;
+  check_cuda(cudaMemcpyAsync(&c, cnt.ptr, 8, cudaMemcpyDeviceToHost, E.stream), "count");
+  check_cuda(cudaStreamSynchronize(E.stream), "sophie germain");
+  return seeds + c;
+}
+
+std::vector<uint64_t> primes_in_range(Engine& E, uint64_t a, uint64_t b, uint64_t max_count) {
+  std::vector<uint64_t> seeds;
+  for (uint64_t q : {2ull, 3ull, 5ull}) if (q >= a && q <= b) seeds.push_back(q);
+  if (b < 7) return seeds;
+  // count first, so an oversized request fails before any bitmap is built
+  uint64_t aa = a, bb = b + 1;
+  const uint64_t total = E.run(1, &aa, &bb)[0].count;
+  if (total > max_count) return std::vector<uint64_t>(max_count + 1, 0);
+  Plan plan;
+  uint64_t nw = 0;
+  const uint32_t* wb = sieve_bitmap(E, plan, a, b + 1, &nw);
+  const uint64_t nblocks = (nw + kExBlockWords - 1) / kExBlockWords;
+  DevBuf bc, bo, outb;
+  bc.reserve(4 * std::max<uint64_t>(nblocks, 1));
+  bo.reserve(8 * std::max<uint64_t>(nblocks, 1));
+  std::vector<uint64_t> res(seeds);
+  if (nblocks) {
+    extract_count_kernel<<<(unsigned)nblocks, kExThreads, 0, E.stream>>>(wb, nw, bc.as<uint32_t>());
+    check_cuda(cudaGetLastError(), "extract_count_kernel");
+    std::vector<uint32_t> counts(nblocks);
+    check_cuda(cudaMemcpyAsync(counts.data(), bc.ptr, 4 * nblocks, cudaMemcpyDeviceToHost, E.stream), "counts");
+    check_cuda(cudaStreamSynchronize(E.stream), "counts");
+    std::vector<uint64_t> offs(nblocks);
+    uint64_t t = 0;
+    for (uint64_t i = 0; i < nblocks; ++i) { offs[i] = t; t += counts[i]; }
+    if (t) {
+      check_cuda(cudaMemcpyAsync(bo.ptr, offs.data(), 8 * nblocks, cudaMemcpyHostToDevice, E.stream), "offsets");
+      outb.reserve(8 * t);
+      extract_write_kernel<<<(unsigned)nblocks, kExThreads, 0, E.stream>>>(
+          wb, nw, plan.host_reqs[0].k_lo, bo.as<uint64_t>(), outb.as<uint64_t>());
+      check_cuda(cudaGetLastError(), "extract_write_kernel");
+      res.resize(seeds.size() + t);
+      check_cuda(cudaMemcpyAsync(res.data() + seeds.size(), outb.ptr, 8 * t, cudaMemcpyDeviceToHost, E.stream), "primes");
+    }
+    check_cuda(cudaStreamSynchronize(E.stream), "in_range");
+  }
+  return res;
+}
+
+}  // namespace vg

@@ -1,0 +1,425 @@
+// sieve.cu -- wheel-30 segmented sieve with fused reductions, for sm_103a.
+//
+// One CTA owns one segment of S bytes (30*S integers) at a time, entirely in
+// shared memory, and walks a static list of (request, segment) work items.
+// Per segment:
+//   1. fill: AND of two presieve tiles (primes 7..17 and 19..31) read at the
+//      segment's phase -- replaces the reference's memset + per-prime
+//      launches for the smallest primes (context.cu:404-414);
+//   2. mark, tier A (37 <= p < split): one warp per prime, lane = (residue
+//      class o, stream h), clears every 4p bytes with shared atomics;
+//   3. mark, tier B (p >= split): one thread per prime, 8 classes, few hits;
+//      both tiers start each stream at max(p^2, segment low) as the
+//      reference's sieve_w30_seg_kernel does (sieve.cu:10-37, start offsets
+//      context.cu:354-388);
+//   4. reduce in the same CTA: popcount (count), masked popcount (p mod 4,
+//      p mod 3), and an ordered gap scan with a warp max-scan carrying the
+//      previous prime, histogram in shared memory -- replaces extract +
+//      thrust::sort + mod4 + gaps kernels (extract.cu:10-39,
+//      chebyshev.cu:11-25, gaps.cu:31-75).
+// Segment boundaries, 2/3/5 and request totals are stitched by
+// finalize_kernel (the reference does this on the host, context.cu:462-524).
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "sieve.cuh"
+
+namespace vg {
+
+__device__ __forceinline__ uint32_t w30(uint32_t o) {
+  return (uint32_t)((kW30Packed >> (o << 3)) & 0xFFu);
+}
+
+// x mod p by Barrett reduction with m = floor((2^64-1)/p).
+__device__ __forceinline__ uint32_t mod_barrett(uint64_t x, uint32_t p, uint64_t m) {
+  uint64_t q = __umul64hi(x, m);
+  uint64_t r = x - q * (uint64_t)p;
+  return (uint32_t)(r >= p ? r - p : r);
+}
+
+// 4 bytes of a tile starting at byte offset `off` (any alignment).
+__device__ __forceinline__ uint32_t tile_word(const uint32_t* __restrict__ t, uint32_t off) {
+  const uint32_t i = off >> 2;
+  const uint32_t lo = __ldg(t + i), hi = __ldg(t + i + 1);
+  return __funnelshift_r(lo, hi, (off & 3u) << 3);
+}
+
+// First hit (segment-local byte) of class o of prime p, moved up so that the
+// number it stands for is >= p*p.  Returns >= nbytes if there is none.
+__device__ __forceinline__ uint32_t lift_to_square(uint32_t s, uint64_t k0, uint32_t p,
+                                                   uint32_t o, uint32_t nbytes) {
+  const uint64_t n = 30ull * (k0 + s) + w30(o);
+  const uint64_t p2 = (uint64_t)p * p;
+  if (n >= p2) return s;
+  const uint64_t step = 30ull * p;
+  const uint64_t add = ((p2 - n + step - 1) / step) * p;
+  const uint64_t s2 = s + add;
+  return s2 < nbytes ? (uint32_t)s2 : nbytes;
+}
+
+__device__ __forceinline__ void clear_bit(uint32_t* seg, uint32_t j, uint32_t o) {
+  atomicAnd(seg + (j >> 2), ~(1u << (((j & 3u) << 3) | o)));
+}
+
+struct GapSink {
+  uint32_t* shist;           // this warp's shared histogram copy
+  ReqAccum* acc;             // this request's global accumulators
+  LargeGapRec* large;
+  unsigned int* n_large;
+  uint32_t cap;
+  uint32_t req;
+  uint64_t base;             // 30 * k0: absolute value of relative 0
+};
+
+__device__ __forceinline__ void record_gap(const GapSink& sk, uint32_t vprev, uint32_t v,
+                                           uint32_t& maxg, uint32_t& maxgs) {
+  const uint32_t g = v - vprev;
+  const uint32_t bin = g >> 1;
+  if (bin < (uint32_t)kSmemBins) {
+    atomicAdd(sk.shist + bin, 1u);
+  } else {
+    atomicAdd(&sk.acc->hist[bin < (uint32_t)kHistBins ? bin : kHistBins - 1], 1ull);
+  }
+  if (g > maxg) { maxg = g; maxgs = vprev; }
+  if (g >= kLargeGap) {
+    const unsigned idx = atomicAdd(sk.n_large, 1u);
+    if (idx < sk.cap) {
+      LargeGapRec r; r.pos = sk.base + v; r.gap = g; r.req = sk.req;
+      sk.large[idx] = r;
+    }
+  }
+}
+
+// Shared-memory per-warp record used to stitch warps inside a segment.
+struct WarpRec {
+  uint32_t first1, last1;    // relative value + 1 (0 = none)
+  uint32_t cnt, c41, c31;
+  uint32_t maxg, maxgs;
+  uint32_t pad;
+};
+
+__global__ void __launch_bounds__(kMaxThreads, 1)
+sieve_segments_kernel(const SieveParams prm) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  uint32_t* seg = smem;
+  uint32_t* shist = seg + (prm.seg_bytes >> 2);
+  WarpRec* wrec = reinterpret_cast<WarpRec*>(shist + kSmemHistCopies * kSmemBins);
+
+  __shared__ uint64_t s_k0, s_seg_in_req;
+  __shared__ uint32_t s_req, s_nbytes, s_np;
+
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t nthr = blockDim.x, nwarps = nthr >> 5;
+
+  for (uint32_t i = tid; i < kSmemHistCopies * kSmemBins; i += nthr) shist[i] = 0;
+  int cur_req = -1;
+
+  for (uint64_t item = blockIdx.x; item < prm.total_segs; item += gridDim.x) {
+    if (tid == 0) {
+      uint32_t lo = 0, hi = prm.nreq;             // last request with seg_base <= item
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (prm.reqs[mid].seg_base <= item) lo = mid; else hi = mid;
+      }
+      const ReqDesc& R = prm.reqs[lo];
+      const uint64_t si = item - R.seg_base;
+      const uint64_t k0 = R.k_lo + si * prm.seg_bytes;
+      const uint64_t left = R.k_hi - k0;
+      const uint32_t nb = left < prm.seg_bytes ? (uint32_t)left : prm.seg_bytes;
+      // table primes with p*p below the segment's upper end
+      const uint64_t hi_num = 30ull * (k0 + nb);
+      uint32_t a = 0, b = R.nprimes;
+      while (a < b) {
+        const uint32_t mid = (a + b) >> 1;
+        const uint64_t p = prm.P[mid];
+        if (p * p < hi_num) a = mid + 1; else b = mid;
+      }
+      s_req = lo; s_k0 = k0; s_seg_in_req = si; s_nbytes = nb; s_np = a;
+    }
+    __syncthreads();
+    const uint32_t req = s_req;
+    const uint64_t k0 = s_k0;
+    const uint32_t nbytes = s_nbytes;
+    const uint32_t nwords = (nbytes + 3u) >> 2;
+    const uint32_t np = s_np;
+
+    if ((int)req != cur_req) {
+      if (cur_req >= 0) {                           // flush the previous request's bins
+        for (uint32_t bn = tid; bn < (uint32_t)kSmemBins; bn += nthr) {
+          uint32_t s = 0;
+#pragma unroll
+          for (int c = 0; c < kSmemHistCopies; ++c) { s += shist[c * kSmemBins + bn]; shist[c * kSmemBins + bn] = 0; }
+          if (s) atomicAdd(&prm.acc[cur_req].hist[bn], (unsigned long long)s);
+        }
+      }
+      cur_req = (int)req;
+    }
+
+    // 1. presieve fill
+    {
+      const uint32_t phA = (uint32_t)(k0 % kTileAPeriod);
+      const uint32_t phB = (uint32_t)(k0 % kTileBPeriod);
+      for (uint32_t w = tid; w < nwords; w += nthr)
+        seg[w] = tile_word(prm.tileA, phA + 4u * w) & tile_word(prm.tileB, phB + 4u * w);
+    }
+    __syncthreads();
+
+    // 2. tier A: warp per prime, lane = (class o, stream h of 4)
+    {
+      const uint32_t ta_end = prm.tier_split < np ? prm.tier_split : np;
+      const uint32_t o = lane & 7u, h = lane >> 3;
+      for (uint32_t i = warp; i < ta_end; i += nwarps) {
+        const uint32_t p = __ldg(prm.P + i);
+        const uint32_t m = mod_barrett(k0, p, __ldg(prm.M + i));
+        const uint32_t r = __ldg(prm.R + o * prm.rstride + i);
+        uint32_t s = r >= m ? r - m : r + p - m;
+        if (30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
+        const uint32_t step = 4u * p;
+        for (uint32_t j = s + h * p; j < nbytes; j += step) clear_bit(seg, j, o);
+      }
+    }
+    // 3. tier B: thread per prime
+    for (uint32_t i = prm.tier_split + tid; i < np; i += nthr) {
+      const uint32_t p = __ldg(prm.P + i);
+      const uint32_t m = mod_barrett(k0, p, __ldg(prm.M + i));
+      const bool low = 30ull * k0 < (uint64_t)p * p;
+#pragma unroll
+      for (uint32_t o = 0; o < 8; ++o) {
+        const uint32_t r = __ldg(prm.R + o * prm.rstride + i);
+        uint32_t s = r >= m ? r - m : r + p - m;
+        if (low) s = lift_to_square(s, k0, p, o, nbytes);
+        for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, o);
+      }
+    }
+    __syncthreads();
+
+    // fix-ups: the tile primes themselves, 1, and the request's edges
+    if (tid == 0) {
+      const ReqDesc& R = prm.reqs[req];
+      if (k0 == 0) seg[0] = (seg[0] & 0xFFFFFE00u) | 0x1FEu;   // 1 no; 7..29, 31 yes
+      if (s_seg_in_req == 0) {
+        uint32_t m = 0;
+        for (uint32_t o = 0; o < 8; ++o) if (30ull * k0 + w30(o) < R.a) m |= 1u << o;
+        seg[0] &= ~m;
+      }
+      if (k0 + nbytes == R.k_hi) {
+        const uint32_t lb = nbytes - 1;
+        uint32_t m = 0;
+        for (uint32_t o = 0; o < 8; ++o) if (30ull * (k0 + lb) + w30(o) >= R.b) m |= 1u << o;
+        seg[lb >> 2] &= ~(m << ((lb & 3u) << 3));
+        const uint32_t rem = nbytes & 3u;
+        if (rem) seg[lb >> 2] &= (1u << (rem << 3)) - 1u;
+      }
+    }
+    __syncthreads();
+
+    if (prm.flags & kFlagBitmap) {
+      uint32_t* dst = prm.bitmap + ((k0 - prm.reqs[0].k_lo) >> 2);
+      for (uint32_t w = tid; w < nwords; w += nthr) dst[w] = seg[w];
+    }
+
+    // 4. reductions: warp-contiguous chunks, lanes on consecutive words
+    {
+      GapSink sk;
+      sk.shist = shist + (warp % kSmemHistCopies) * kSmemBins;
+      sk.acc = prm.acc + req;
+      sk.large = prm.large; sk.n_large = prm.n_large; sk.cap = prm.large_cap;
+      sk.req = req; sk.base = 30ull * k0;
+      const uint32_t m41 = (k0 & 1ull) ? 0x99669966u : 0x66996699u;
+      const uint32_t per = (((nwords + nwarps - 1) / nwarps) + 31u) & ~31u;
+      const uint32_t wbeg = warp * per;
+      const uint32_t wend = min(wbeg + per, nwords);
+      uint32_t carry = 0, wfirst = 0, cnt = 0, c41 = 0, c31 = 0, maxg = 0, maxgs = 0;
+      for (uint32_t base = wbeg; base < wend; base += 32) {
+        const uint32_t wi = base + lane;
+        const uint32_t word = wi < wend ? seg[wi] : 0u;
+        cnt += __popc(word);
+        c41 += __popc(word & m41);
+        c31 += __popc(word & 0x2B2B2B2Bu);
+        uint32_t last1 = 0;
+        if (word) {
+          const uint32_t hb = 31u - __clz(word);
+          last1 = 30u * (4u * wi + (hb >> 3)) + w30(hb & 7u) + 1u;
+        }
+        uint32_t sc = last1;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, sc, d);
+          if ((int)lane >= d) sc = max(sc, t);
+        }
+        uint32_t prev1 = __shfl_up_sync(0xFFFFFFFFu, sc, 1);
+        if (lane == 0) prev1 = 0;
+        prev1 = max(prev1, carry);
+        carry = max(carry, __shfl_sync(0xFFFFFFFFu, sc, 31));
+        uint32_t w = word;
+        while (w) {
+          const uint32_t bp = (uint32_t)__ffs(w) - 1u;
+          w &= w - 1u;
+          const uint32_t v = 30u * (4u * wi + (bp >> 3)) + w30(bp & 7u);
+          if (prev1) record_gap(sk, prev1 - 1u, v, maxg, maxgs);
+          else wfirst = v + 1u;
+          prev1 = v + 1u;
+        }
+      }
+      cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
+      c41 = __reduce_add_sync(0xFFFFFFFFu, c41);
+      c31 = __reduce_add_sync(0xFFFFFFFFu, c31);
+      wfirst = __reduce_max_sync(0xFFFFFFFFu, wfirst);
+      const uint32_t gm = __reduce_max_sync(0xFFFFFFFFu, maxg);
+      const uint32_t gs = __reduce_min_sync(0xFFFFFFFFu, (maxg == gm && gm) ? maxgs : 0xFFFFFFFFu);
+      if (lane == 0) {
+        WarpRec r;
+        r.first1 = wfirst; r.last1 = carry; r.cnt = cnt; r.c41 = c41; r.c31 = c31;
+        r.maxg = gm; r.maxgs = gs; r.pad = 0;
+        wrec[warp] = r;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        uint32_t run1 = 0, first1 = 0, tc = 0, t41 = 0, t31 = 0, bg = 0, bs = 0;
+        for (uint32_t wv = 0; wv < nwarps; ++wv) {
+          const WarpRec r = wrec[wv];
+          if (r.first1) {
+            if (run1) record_gap(sk, run1 - 1u, r.first1 - 1u, bg, bs);
+            else first1 = r.first1;
+            run1 = r.last1;
+          }
+          if (r.maxg > bg || (r.maxg == bg && r.maxg && r.maxgs < bs)) { bg = r.maxg; bs = r.maxgs; }
+          tc += r.cnt; t41 += r.c41; t31 += r.c31;
+        }
+        SegRec sr;
+        sr.first = first1 ? sk.base + first1 - 1u : 0;
+        sr.last = run1 ? sk.base + run1 - 1u : 0;
+        sr.max_gap = bg;
+        sr.max_gap_start = bg ? sk.base + bs : 0;
+        sr.count = tc;
+        prm.segs[item] = sr;
+        if (tc) {
+          atomicAdd(&sk.acc->count, (unsigned long long)tc);
+          atomicAdd(&sk.acc->c41, (unsigned long long)t41);
+          atomicAdd(&sk.acc->c31, (unsigned long long)t31);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (cur_req >= 0) {
+    for (uint32_t bn = tid; bn < (uint32_t)kSmemBins; bn += nthr) {
+      uint32_t s = 0;
+#pragma unroll
+      for (int c = 0; c < kSmemHistCopies; ++c) s += shist[c * kSmemBins + bn];
+      if (s) atomicAdd(&prm.acc[cur_req].hist[bn], (unsigned long long)s);
+    }
+  }
+}
+
+// One CTA per request: seeds 2, 3, 5, gaps across segment boundaries, the
+// largest gap, and the final counts (the reference's host-side conventions,
+// context.cu:321-322,462-524, restated for a half-open [a, b)).
+__global__ void __launch_bounds__(256)
+finalize_kernel(const ReqDesc* __restrict__ reqs, const SegRec* __restrict__ segs,
+                ReqAccum* __restrict__ acc, LargeGapRec* large, unsigned int* n_large,
+                uint32_t large_cap, ReqResult* __restrict__ out) {
+  const uint32_t r = blockIdx.x, tid = threadIdx.x;
+  const ReqDesc R = reqs[r];
+  ReqAccum* A = acc + r;
+  const SegRec* S = segs + R.seg_base;
+  __shared__ uint64_t s_bg[256], s_bs[256];
+
+  const bool in2 = R.a <= 2 && 2 < R.b, in3 = R.a <= 3 && 3 < R.b, in5 = R.a <= 5 && 5 < R.b;
+  const uint64_t seed_first = in2 ? 2 : in3 ? 3 : in5 ? 5 : 0;
+  const uint64_t seed_last = in5 ? 5 : in3 ? 3 : in2 ? 2 : 0;
+
+  uint64_t bg = 0, bs = 0;
+  auto consider = [&](uint64_t g, uint64_t st) {
+    if (g > bg || (g == bg && g && st < bs)) { bg = g; bs = st; }
+  };
+  if (tid == 0) {
+    if (in2 && in3) { atomicAdd(&A->hist[0], 1ull); consider(1, 2); }
+    if (in3 && in5) { atomicAdd(&A->hist[1], 1ull); consider(2, 3); }
+  }
+  for (uint64_t i = tid; i < R.nseg; i += blockDim.x) {
+    const SegRec s = S[i];
+    if (s.max_gap) consider(s.max_gap, s.max_gap_start);
+    if (!s.first) continue;
+    uint64_t prev = 0;
+    for (uint64_t j = i; j-- > 0;) {
+      if (S[j].first) { prev = S[j].last; break; }
+    }
+    if (!prev) prev = seed_last;
+    if (!prev) continue;
+    const uint64_t g = s.first - prev;
+    const uint64_t bin = g >> 1;
+    atomicAdd(&A->hist[bin < (uint64_t)kHistBins ? bin : kHistBins - 1], 1ull);
+    consider(g, prev);
+    if (g >= kLargeGap) {
+      const unsigned idx = atomicAdd(n_large, 1u);
+      if (idx < large_cap) {
+        LargeGapRec lr; lr.pos = s.first; lr.gap = (uint32_t)g; lr.req = r;
+        large[idx] = lr;
+      }
+    }
+  }
+  s_bg[tid] = bg; s_bs[tid] = bs;
+  __syncthreads();
+  for (uint32_t w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (tid < w) {
+      const uint64_t g2 = s_bg[tid + w], t2 = s_bs[tid + w];
+      if (g2 > s_bg[tid] || (g2 == s_bg[tid] && g2 && t2 < s_bs[tid])) { s_bg[tid] = g2; s_bs[tid] = t2; }
+    }
+    __syncthreads();
+  }
+  ReqResult* O = out + r;
+  for (uint32_t b = tid; b < (uint32_t)kHistBins; b += blockDim.x) O->hist[b] = A->hist[b];
+  if (tid == 0) {
+    const uint64_t ns = (uint64_t)in2 + in3 + in5;
+    const uint64_t wc = A->count;
+    O->count = wc + ns;
+    O->c41 = A->c41 + (in5 ? 1 : 0);
+    O->c43 = (wc - A->c41) + (in3 ? 1 : 0);
+    O->c31 = A->c31;
+    O->c32 = (wc - A->c31) + (in2 ? 1 : 0) + (in5 ? 1 : 0);
+    uint64_t f = seed_first, l = seed_last;
+    if (!f) {
+      for (uint64_t i = 0; i < R.nseg; ++i) if (S[i].first) { f = S[i].first; break; }
+    }
+    for (uint64_t i = R.nseg; i-- > 0;) if (S[i].last) { l = S[i].last; break; }
+    O->first = f;
+    O->last = l;
+    O->max_gap = s_bg[0];
+    O->max_gap_start = s_bg[0] ? s_bs[0] : 0;
+    O->num_gaps = O->count ? O->count - 1 : 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers (called by the engine)
+// ---------------------------------------------------------------------------
+size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads) {
+  return (size_t)seg_bytes + sizeof(uint32_t) * kSmemHistCopies * kSmemBins +
+         sizeof(WarpRec) * (threads / 32);
+}
+
+cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads,
+                         cudaStream_t stream) {
+  const size_t smem = sieve_smem_bytes(prm.seg_bytes, threads);
+  static size_t smem_set = 0;   // the attribute is raised once, before any capture
+  if (smem > smem_set) {
+    cudaError_t e = cudaFuncSetAttribute(sieve_segments_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    smem_set = smem;
+  }
+  if (grid == 0 || prm.total_segs == 0) return cudaSuccess;
+  sieve_segments_kernel<<<grid, threads, smem, stream>>>(prm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const ReqDesc* reqs, const SegRec* segs, ReqAccum* acc,
+                            LargeGapRec* large, unsigned int* n_large, uint32_t large_cap,
+                            ReqResult* out, uint32_t nreq, cudaStream_t stream) {
+  if (nreq == 0) return cudaSuccess;
+  finalize_kernel<<<nreq, 256, 0, stream>>>(reqs, segs, acc, large, n_large, large_cap, out);
+  return cudaGetLastError();
+}
+
+}  // namespace vg

@@ -1,0 +1,91 @@
+// sieve.cuh -- shared layouts of the wheel-30 segmented sieve (device + host).
+//
+// Bit layout (the reference's, src/voss_w30_v7.cu:38-39 and
+// library/src/primes/context.cu:469-470): byte k of the wheel covers the 30
+// integers 30k .. 30k+29; bit o of that byte stands for 30k + W30[o] with
+// W30 = {1, 7, 11, 13, 17, 19, 23, 29}.  Four bytes form one little-endian
+// uint32 word, so bit (k & 3) * 8 + o of word k / 4 is the same bit index
+// k * 8 + o that the reference's uint32 `bits` array uses.
+#pragma once
+#include <cstdint>
+
+namespace vg {
+
+constexpr uint64_t kW30Packed = 0x1D1713110D0B0701ull;  // W30[o] = byte o
+constexpr int kHistBins = 1025;       // gap/2 bins 0..1023, bin 1024 = gap >= 2048
+constexpr int kSmemBins = 256;        // bins kept in shared memory (gap < 512)
+constexpr int kSmemHistCopies = 8;    // one copy per 4 warps
+constexpr uint32_t kLargeGap = 500;   // the reference's large-gap threshold
+constexpr uint32_t kTileAPeriod = 7u * 11u * 13u * 17u;      // 17017 bytes
+constexpr uint32_t kTileBPeriod = 19u * 23u * 29u * 31u;     // 392863 bytes
+constexpr uint32_t kFirstTablePrime = 37;   // smallest prime not in a tile
+constexpr int kMaxThreads = 1024;
+
+// Flags of one launch.
+constexpr uint32_t kFlagBitmap = 1u;     // also write the sieved words out
+
+// One range request, half-open [a, b), as the device sees it.
+struct ReqDesc {
+  uint64_t a, b;
+  uint64_t k_lo, k_hi;      // wheel bytes [k_lo, k_hi) that cover [a, b)
+  uint64_t seg_base;        // index of the request's first segment
+  uint64_t nseg;
+  uint32_t nprimes;         // table primes p (>= 37) with p*p < b
+  uint32_t pad;
+};
+
+// Per segment: first/last prime (absolute, 0 = none), the largest gap
+// strictly inside the segment and its first prime, the prime count.
+struct SegRec {
+  uint64_t first, last;
+  uint64_t max_gap_start;
+  uint32_t max_gap;
+  uint32_t count;
+};
+
+// Per request accumulators (global atomics).  Counts are of wheel primes
+// (>= 7) only; the finalize step adds 2, 3, 5.
+struct ReqAccum {
+  unsigned long long count, c41, c31;
+  unsigned long long hist[kHistBins];
+};
+
+// A gap >= kLargeGap: position = second prime (the reference's convention).
+struct LargeGapRec {
+  uint64_t pos;
+  uint32_t gap;
+  uint32_t req;
+};
+
+// Final per request result, written by the finalize kernel.
+struct ReqResult {
+  uint64_t count;
+  uint64_t c41, c43, c31, c32;
+  uint64_t first, last;
+  uint64_t max_gap, max_gap_start;
+  uint64_t num_gaps;
+  uint64_t hist[kHistBins];
+};
+
+struct SieveParams {
+  const ReqDesc* reqs;
+  uint32_t nreq;
+  uint64_t total_segs;
+  const uint32_t* P;         // table primes >= 37, ascending
+  const uint64_t* M;         // floor((2^64-1)/p), for x mod p
+  const uint32_t* R;         // R[o * rstride + i]: k = R (mod p) <=> p | 30k+W30[o]
+  uint64_t rstride;
+  const uint32_t* tileA;     // presieve tiles, extended past their period
+  const uint32_t* tileB;
+  uint32_t seg_bytes;        // S, a multiple of 128
+  uint32_t tier_split;       // table index of the first thread-per-prime prime
+  SegRec* segs;
+  ReqAccum* acc;
+  LargeGapRec* large;
+  unsigned int* n_large;
+  uint32_t large_cap;
+  uint32_t flags;
+  uint32_t* bitmap;          // kFlagBitmap: words of request 0, from k_lo
+};
+
+}  // namespace vg
