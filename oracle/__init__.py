@@ -39,7 +39,7 @@ def build(force: bool = False) -> Path:
             and LIB_PATH.stat().st_mtime >= max(src.stat().st_mtime, hdr.stat().st_mtime)):
         return LIB_PATH
     tmp = LIB_PATH.with_suffix(".so.tmp%d" % os.getpid())
-    subprocess.check_call(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11",
+    subprocess.check_call(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off",
                            "-o", str(tmp), str(src)])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH

@@ -173,9 +173,18 @@ def test_progress_callback_chunks(vg):
     seen = []
     with vg.Context(N, profile="minimal") as c1, vg.Context(N, profile="minimal") as c2:
         c1.set_progress(lambda *a: seen.append(a))
-        assert c1.prime_count() == c2.prime_count()
+        pi = c2.prime_count()
+        assert c1.prime_count() == pi
     assert [s[:2] for s in seen] == [(1, 3), (2, 3), (3, 3)]
-    assert seen[-1][3] == c2.prime_count() and sum(s[2] for s in seen) + 3 == seen[-1][3]
+    assert seen[-1][3] == pi and sum(s[2] for s in seen) + 3 == seen[-1][3]
+    seen = []
+    with vg.Context(N) as c1, vg.Context(N) as c2:       # full statistics, chunked vs whole
+        c1.set_progress(lambda *a: seen.append(a))
+        s1, s2 = c1.statistics(), c2.statistics()
+        assert (s1.mean_gap, s1.std_dev, s1.skewness, s1.kurtosis, s1.total_gaps) == (
+            s2.mean_gap, s2.std_dev, s2.skewness, s2.kurtosis, s2.total_gaps)
+        assert c1.large_gaps() == c2.large_gaps() and c1.twins() == c2.twins()
+        assert (c1.chebyshev().pi_4_1, c1.chebyshev().pi_4_3) == (c2.chebyshev().pi_4_1, c2.chebyshev().pi_4_3)
 
 
 def test_in_range(vg, oracle_lib):

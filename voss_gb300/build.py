@@ -37,7 +37,10 @@ def cuda_lib_dir() -> str:
 
 
 def _flags() -> list[str]:
-    return ["-O3", "-std=c++17", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-Wall",
+    # -ffp-contract=off: host doubles (gap moments) must not be fused into FMAs,
+    # which g++ does by default on aarch64 but not on x86; the reference's
+    # statistics are plain multiply-then-add.
+    return ["-O3", "-std=c++17", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-Wall,-ffp-contract=off",
             "-I", str(ROOT / "include"), "-I", str(CSRC)]
 
 

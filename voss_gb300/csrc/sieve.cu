@@ -196,7 +196,9 @@ sieve_segments_kernel(const SieveParams prm) {
     // fix-ups: the tile primes themselves, 1, and the request's edges
     if (tid == 0) {
       const ReqDesc& R = prm.reqs[req];
+      // The tiles clear their own primes: 7..29 live in byte 0, 31 in byte 1.
       if (k0 == 0) seg[0] = (seg[0] & 0xFFFFFE00u) | 0x1FEu;   // 1 no; 7..29, 31 yes
+      else if (k0 == 1) seg[0] |= 1u;                            // 31
       if (s_seg_in_req == 0) {
         uint32_t m = 0;
         for (uint32_t o = 0; o < 8; ++o) if (30ull * k0 + w30(o) < R.a) m |= 1u << o;
