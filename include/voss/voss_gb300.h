@@ -59,7 +59,7 @@ int voss_primes_range_stats_batch(uint64_t n, const uint64_t* a, const uint64_t*
 /* Tunables of the segmented sieve.  seg_bytes: shared-memory segment in
  * bytes (30 integers each), a multiple of 128, at most 196608.  threads: CTA
  * size (multiple of 32, <= 1024).  tier_split: primes below it are marked a
- * warp per prime, primes above it a thread per prime.  ctas_per_sm: resident
+ * warp per prime, primes from it on four primes per warp.  ctas_per_sm: resident
  * CTAs per SM used to size the persistent grid.  Zero fields keep the
  * current value; auto_tune = 1 lets the library pick per range. */
 typedef struct {

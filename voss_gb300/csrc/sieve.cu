@@ -6,13 +6,13 @@
 //   1. fill: AND of two presieve tiles (primes 7..17 and 19..31) read at the
 //      segment's phase -- replaces the reference's memset + per-prime
 //      launches for the smallest primes (context.cu:404-414);
-//   2. mark, tier A (37 <= p < split): one warp per prime, lane = (residue
-//      class o, stream h), clears every 4p bytes with shared atomics;
-//   3. mark, tier B (p >= split): one thread per prime, 8 classes, few hits;
-//      both tiers start each stream at max(p^2, segment low) as the
-//      reference's sieve_w30_seg_kernel does (sieve.cu:10-37, start offsets
-//      context.cu:354-388);
-//   4. reduce in the same CTA: popcount (count), masked popcount (p mod 4,
+//   2. mark with shared-memory atomicAnd, in work units handed out heaviest
+//      first by a shared counter: primes 37 <= p < split one warp each
+//      (lane = residue class x stream, fixed bit mask per stream), primes
+//      p >= split four per warp (lane = prime x class).  Each stream starts
+//      at max(p^2, segment low), as the reference's sieve_w30_seg_kernel
+//      does (sieve.cu:10-37, start offsets context.cu:354-388);
+//   3. reduce in the same CTA: popcount (count), masked popcount (p mod 4,
 //      p mod 3), and an ordered gap scan with a warp max-scan carrying the
 //      previous prime, histogram in shared memory -- replaces extract +
 //      thrust::sort + mod4 + gaps kernels (extract.cu:10-39,
@@ -106,12 +106,15 @@ sieve_segments_kernel(const SieveParams prm) {
   WarpRec* wrec = reinterpret_cast<WarpRec*>(shist + kSmemHistCopies * kSmemBins);
 
   __shared__ uint64_t s_k0, s_seg_in_req;
-  __shared__ uint32_t s_req, s_nbytes, s_np;
+  __shared__ uint32_t s_req, s_nbytes, s_np, s_ctr;
+  __shared__ uint32_t s_vtab[32];      // bit b of a word -> 30*(b/8) + W30[b%8]
 
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t nthr = blockDim.x, nwarps = nthr >> 5;
 
   for (uint32_t i = tid; i < kSmemHistCopies * kSmemBins; i += nthr) shist[i] = 0;
+  if (tid < 32) s_vtab[tid] = 30u * (tid >> 3) + w30(tid & 7u);
+  if (tid == 0) s_ctr = 0;
   int cur_req = -1;
 
   for (uint64_t item = blockIdx.x; item < prm.total_segs; item += gridDim.x) {
@@ -164,31 +167,59 @@ sieve_segments_kernel(const SieveParams prm) {
     }
     __syncthreads();
 
-    // 2. tier A: warp per prime, lane = (class o, stream h of 4)
+    // 2. marking.  Work units, heaviest first, handed out by a shared counter:
+    //    units [0, nsmall): one prime each, p < split: a warp per prime, lane
+    //      = (class o, stream h of 4); a stream steps 4p bytes = p words, so
+    //      its bit mask never changes;
+    //    units [nsmall, ...): 32 primes each, p >= split: lanes = (prime q of
+    //      4, class o), eight rounds of four primes, loads of all rounds
+    //      issued before any marking so their latency overlaps.
     {
-      const uint32_t ta_end = prm.tier_split < np ? prm.tier_split : np;
+      const uint32_t nsmall = prm.tier_split < np ? prm.tier_split : np;
+      const uint32_t nunits = nsmall + (np - nsmall + 31u) / 32u;
       const uint32_t o = lane & 7u, h = lane >> 3;
-      for (uint32_t i = warp; i < ta_end; i += nwarps) {
-        const uint32_t p = __ldg(prm.P + i);
-        const uint32_t m = mod_barrett(k0, p, __ldg(prm.M + i));
-        const uint32_t r = __ldg(prm.R + o * prm.rstride + i);
-        uint32_t s = r >= m ? r - m : r + p - m;
-        if (30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
-        const uint32_t step = 4u * p;
-        for (uint32_t j = s + h * p; j < nbytes; j += step) clear_bit(seg, j, o);
-      }
-    }
-    // 3. tier B: thread per prime
-    for (uint32_t i = prm.tier_split + tid; i < np; i += nthr) {
-      const uint32_t p = __ldg(prm.P + i);
-      const uint32_t m = mod_barrett(k0, p, __ldg(prm.M + i));
-      const bool low = 30ull * k0 < (uint64_t)p * p;
+      for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(&s_ctr, 1u);
+        u = __shfl_sync(0xFFFFFFFFu, u, 0);
+        if (u >= nunits) break;
+        if (u < nsmall) {
+          const uint32_t p = __ldg(prm.P + u);
+          const uint32_t m = mod_barrett(k0, p, __ldg(prm.M + u));
+          const uint32_t r = __ldg(prm.R + o * prm.rstride + u);
+          uint32_t s = r >= m ? r - m : r + p - m;
+          if (30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
+          const uint32_t j0 = s + h * p;
+          if (j0 < nbytes) {
+            const uint32_t c = j0 & 3u;
+            const uint32_t mask = ~(1u << ((c << 3) | o));
+            const uint32_t lim = (nbytes - c + 3u) >> 2;
+            uint32_t w = j0 >> 2;
+#pragma unroll 4
+            for (; w < lim; w += p) atomicAnd(seg + w, mask);
+          }
+        } else {
+          const uint32_t base = nsmall + 32u * (u - nsmall);
+          uint32_t pp[8], rr[8];
+          uint64_t mm[8];
 #pragma unroll
-      for (uint32_t o = 0; o < 8; ++o) {
-        const uint32_t r = __ldg(prm.R + o * prm.rstride + i);
-        uint32_t s = r >= m ? r - m : r + p - m;
-        if (low) s = lift_to_square(s, k0, p, o, nbytes);
-        for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, o);
+          for (int t = 0; t < 8; ++t) {
+            const uint32_t i = base + 4u * t + h;
+            const bool ok = i < np;
+            pp[t] = ok ? __ldg(prm.P + i) : 0u;
+            mm[t] = ok ? __ldg(prm.M + i) : 0ull;
+            rr[t] = ok ? __ldg(prm.R + o * prm.rstride + i) : 0u;
+          }
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const uint32_t p = pp[t];
+            if (!p) continue;
+            const uint32_t m = mod_barrett(k0, p, mm[t]);
+            uint32_t s = rr[t] >= m ? rr[t] - m : rr[t] + p - m;
+            if (30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
+            for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, o);
+          }
+        }
       }
     }
     __syncthreads();
@@ -212,6 +243,7 @@ sieve_segments_kernel(const SieveParams prm) {
         const uint32_t rem = nbytes & 3u;
         if (rem) seg[lb >> 2] &= (1u << (rem << 3)) - 1u;
       }
+      s_ctr = 0;                                   // for the next segment's marking
     }
     __syncthreads();
 
@@ -220,7 +252,9 @@ sieve_segments_kernel(const SieveParams prm) {
       for (uint32_t w = tid; w < nwords; w += nthr) dst[w] = seg[w];
     }
 
-    // 4. reductions: warp-contiguous chunks, lanes on consecutive words
+    // 3. reductions: each thread scans one contiguous run of words (odd
+    //    length, so the lanes of a warp hit distinct banks); lanes are
+    //    stitched with a warp max-scan of their last prime, warps by thread 0.
     {
       GapSink sk;
       sk.shist = shist + (warp % kSmemHistCopies) * kSmemBins;
@@ -228,68 +262,65 @@ sieve_segments_kernel(const SieveParams prm) {
       sk.large = prm.large; sk.n_large = prm.n_large; sk.cap = prm.large_cap;
       sk.req = req; sk.base = 30ull * k0;
       const uint32_t m41 = (k0 & 1ull) ? 0x99669966u : 0x66996699u;
-      const uint32_t per = (((nwords + nwarps - 1) / nwarps) + 31u) & ~31u;
-      const uint32_t wbeg = warp * per;
-      const uint32_t wend = min(wbeg + per, nwords);
-      uint32_t carry = 0, wfirst = 0, cnt = 0, c41 = 0, c31 = 0, maxg = 0, maxgs = 0;
-      for (uint32_t base = wbeg; base < wend; base += 32) {
-        const uint32_t wi = base + lane;
-        const uint32_t word = wi < wend ? seg[wi] : 0u;
-        cnt += __popc(word);
-        c41 += __popc(word & m41);
-        c31 += __popc(word & 0x2B2B2B2Bu);
-        uint32_t last1 = 0;
-        if (word) {
-          const uint32_t hb = 31u - __clz(word);
-          last1 = 30u * (4u * wi + (hb >> 3)) + w30(hb & 7u) + 1u;
-        }
-        uint32_t sc = last1;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, sc, d);
-          if ((int)lane >= d) sc = max(sc, t);
-        }
-        uint32_t prev1 = __shfl_up_sync(0xFFFFFFFFu, sc, 1);
-        if (lane == 0) prev1 = 0;
-        prev1 = max(prev1, carry);
-        carry = max(carry, __shfl_sync(0xFFFFFFFFu, sc, 31));
-        uint32_t w = word;
-        while (w) {
+      const uint32_t run = ((nwords + nthr - 1) / nthr) | 1u;
+      const uint32_t wbeg = min(tid * run, nwords);
+      const uint32_t wend = min(wbeg + run, nwords);
+      uint32_t first1 = 0, last1 = 0, cnt = 0, c41 = 0, c31 = 0, maxg = 0, maxgs = 0;
+      for (uint32_t wi = wbeg; wi < wend; ++wi) {
+        uint32_t w = seg[wi];
+        if (!w) continue;
+        cnt += __popc(w);
+        c41 += __popc(w & m41);
+        c31 += __popc(w & 0x2B2B2B2Bu);
+        const uint32_t vb = 120u * wi;
+        do {
           const uint32_t bp = (uint32_t)__ffs(w) - 1u;
           w &= w - 1u;
-          const uint32_t v = 30u * (4u * wi + (bp >> 3)) + w30(bp & 7u);
-          if (prev1) record_gap(sk, prev1 - 1u, v, maxg, maxgs);
-          else wfirst = v + 1u;
-          prev1 = v + 1u;
-        }
+          const uint32_t v = vb + s_vtab[bp];
+          if (last1) record_gap(sk, last1 - 1u, v, maxg, maxgs);
+          else first1 = v + 1u;
+          last1 = v + 1u;
+        } while (w);
       }
+      // lane stitching: previous lane's last prime (values grow with the lane)
+      uint32_t sc = last1;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, sc, d);
+        if ((int)lane >= d) sc = max(sc, t);
+      }
+      uint32_t prev1 = __shfl_up_sync(0xFFFFFFFFu, sc, 1);
+      if (lane == 0) prev1 = 0;
+      if (first1 && prev1) record_gap(sk, prev1 - 1u, first1 - 1u, maxg, maxgs);
+      const uint32_t wlast = __shfl_sync(0xFFFFFFFFu, sc, 31);
+      const uint32_t wfirst = __reduce_min_sync(0xFFFFFFFFu, first1 ? first1 : 0xFFFFFFFFu);
       cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
       c41 = __reduce_add_sync(0xFFFFFFFFu, c41);
       c31 = __reduce_add_sync(0xFFFFFFFFu, c31);
-      wfirst = __reduce_max_sync(0xFFFFFFFFu, wfirst);
       const uint32_t gm = __reduce_max_sync(0xFFFFFFFFu, maxg);
       const uint32_t gs = __reduce_min_sync(0xFFFFFFFFu, (maxg == gm && gm) ? maxgs : 0xFFFFFFFFu);
       if (lane == 0) {
         WarpRec r;
-        r.first1 = wfirst; r.last1 = carry; r.cnt = cnt; r.c41 = c41; r.c31 = c31;
+        r.first1 = wfirst == 0xFFFFFFFFu ? 0u : wfirst;
+        r.last1 = wlast; r.cnt = cnt; r.c41 = c41; r.c31 = c31;
         r.maxg = gm; r.maxgs = gs; r.pad = 0;
         wrec[warp] = r;
       }
       __syncthreads();
       if (tid == 0) {
-        uint32_t run1 = 0, first1 = 0, tc = 0, t41 = 0, t31 = 0, bg = 0, bs = 0;
+        uint32_t run1 = 0, fst1 = 0, tc = 0, t41 = 0, t31 = 0, bg = 0, bs = 0;
         for (uint32_t wv = 0; wv < nwarps; ++wv) {
           const WarpRec r = wrec[wv];
           if (r.first1) {
             if (run1) record_gap(sk, run1 - 1u, r.first1 - 1u, bg, bs);
-            else first1 = r.first1;
+            else fst1 = r.first1;
             run1 = r.last1;
           }
           if (r.maxg > bg || (r.maxg == bg && r.maxg && r.maxgs < bs)) { bg = r.maxg; bs = r.maxgs; }
           tc += r.cnt; t41 += r.c41; t31 += r.c31;
         }
         SegRec sr;
-        sr.first = first1 ? sk.base + first1 - 1u : 0;
+        sr.first = fst1 ? sk.base + fst1 - 1u : 0;
         sr.last = run1 ? sk.base + run1 - 1u : 0;
         sr.max_gap = bg;
         sr.max_gap_start = bg ? sk.base + bs : 0;
