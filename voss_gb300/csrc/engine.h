@@ -53,7 +53,7 @@ struct HostPinned {
 struct Config {
   uint32_t seg_bytes = 196608;
   uint32_t threads = 1024;
-  uint32_t tier_split = 24576;   // primes below: a warp per prime; above: 4 per warp
+  uint32_t tier_split = 6144;    // primes below: a warp per prime; above: 4 per warp
   uint32_t ctas_per_sm = 1;
   uint32_t auto_tune = 1;
 };

@@ -199,24 +199,27 @@ sieve_segments_kernel(const SieveParams prm) {
             for (; w < lim; w += p) atomicAnd(seg + w, mask);
           }
         } else {
+          // p and k0 mod p once per prime (lane = prime), then shuffled to the
+          // (prime, class) lanes of each round.
           const uint32_t base = nsmall + 32u * (u - nsmall);
-          uint32_t pp[8], rr[8];
-          uint64_t mm[8];
+          const uint32_t im = base + lane;
+          const bool okm = im < np;
+          const uint32_t pm = okm ? __ldg(prm.P + im) : 0u;
+          const uint32_t mm = okm ? mod_barrett(k0, pm, __ldg(prm.M + im)) : 0u;
+          const bool low_any = __any_sync(0xFFFFFFFFu, okm && 30ull * k0 < (uint64_t)pm * pm);
+          uint32_t rr[8];
 #pragma unroll
           for (int t = 0; t < 8; ++t) {
             const uint32_t i = base + 4u * t + h;
-            const bool ok = i < np;
-            pp[t] = ok ? __ldg(prm.P + i) : 0u;
-            mm[t] = ok ? __ldg(prm.M + i) : 0ull;
-            rr[t] = ok ? __ldg(prm.R + o * prm.rstride + i) : 0u;
+            rr[t] = i < np ? __ldg(prm.R + o * prm.rstride + i) : 0u;
           }
 #pragma unroll
           for (int t = 0; t < 8; ++t) {
-            const uint32_t p = pp[t];
+            const uint32_t p = __shfl_sync(0xFFFFFFFFu, pm, 4 * t + h);
+            const uint32_t m = __shfl_sync(0xFFFFFFFFu, mm, 4 * t + h);
             if (!p) continue;
-            const uint32_t m = mod_barrett(k0, p, mm[t]);
             uint32_t s = rr[t] >= m ? rr[t] - m : rr[t] + p - m;
-            if (30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
+            if (low_any && 30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
             for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, o);
           }
         }
