@@ -57,7 +57,7 @@ int voss_primes_range_stats_batch(uint64_t n, const uint64_t* a, const uint64_t*
                                   voss_range_stats_t* out);
 
 /* Tunables of the segmented sieve.  seg_bytes: shared-memory segment in
- * bytes (30 integers each), a multiple of 128, at most 196608.  threads: CTA
+ * bytes (30 integers each), a multiple of 128, at most 221184.  threads: CTA
  * size (multiple of 32, <= 1024).  tier_split: primes below it are marked a
  * warp per prime, primes from it on four primes per warp.  ctas_per_sm: resident
  * CTAs per SM used to size the persistent grid.  Zero fields keep the

@@ -94,7 +94,8 @@ def test_minimal_profile_counts(vg):
 def test_random_windows_vs_oracle(vg, oracle_lib):
     rng = random.Random(7)
     cases = [(0, 1), (0, 2), (0, 7), (0, 8), (1, 60), (29, 31), (30, 31), (31, 32), (0, 30 * 196608 + 1),
-             (30 * 196608 - 5, 30 * 196608 + 5), (10**14 - 10**6, 10**14), (10**14, 10**14 + 10**6),
+             (30 * 196608 - 5, 30 * 196608 + 5), (0, 30 * 221184 + 1), (30 * 221184 - 5, 30 * 221184 + 5),
+             (30 * 2 * 221184 - 31, 30 * 2 * 221184 + 29), (10**14 - 10**6, 10**14), (10**14, 10**14 + 10**6),
              (10**14 + 10**10 - 10**5, 10**14 + 10**10 + 1), (2, 3), (3, 5), (5, 6)]
     for _ in range(80):
         a = rng.randrange(0, 10**13)

@@ -223,6 +223,7 @@ void Plan::prepare(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl
   if (!E.cfg.auto_tune) cfg = E.cfg;
   if (max_b > 1) E.ensure_table(isqrt_u64(max_b - 1));
   tier_split_idx = E.index_of(cfg.tier_split);
+  tier_huge_idx = E.index_of(cfg.seg_bytes);
 
   host_reqs.assign(n, ReqDesc{});
   uint64_t segs_total = 0;
@@ -286,6 +287,7 @@ void Plan::launch(cudaStream_t s) {
   prm.tileB = E.tileB.as<uint32_t>();
   prm.seg_bytes = cfg.seg_bytes;
   prm.tier_split = tier_split_idx;
+  prm.tier_huge = tier_huge_idx;
   prm.segs = segs.as<SegRec>();
   prm.acc = acc.as<ReqAccum>();
   prm.large = large.as<LargeGapRec>();

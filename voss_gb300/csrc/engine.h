@@ -51,7 +51,7 @@ struct HostPinned {
 };
 
 struct Config {
-  uint32_t seg_bytes = 196608;
+  uint32_t seg_bytes = 221184;    // 216 KiB: the largest that fits with the histograms
   uint32_t threads = 1024;
   uint32_t tier_split = 6144;    // primes below: a warp per prime; above: 4 per warp
   uint32_t ctas_per_sm = 1;
@@ -68,6 +68,7 @@ struct Plan {
   uint32_t grid = 0;
   Config cfg;
   uint32_t tier_split_idx = 0;
+  uint32_t tier_huge_idx = 0;
   std::vector<ReqDesc> host_reqs;
   DevBuf reqs, segs, acc, large, nlarge, results, bitmap;
   HostPinned host_results;

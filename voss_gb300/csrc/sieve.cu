@@ -71,21 +71,25 @@ struct GapSink {
   uint64_t base;             // 30 * k0: absolute value of relative 0
 };
 
+// Count the gap v - vprev.  Shared bins hold gap/2 < kSmemBins; one extra
+// shared bin (never flushed) absorbs larger gaps, which take the rare path
+// together with a new maximum and gaps >= kLargeGap.
 __device__ __forceinline__ void record_gap(const GapSink& sk, uint32_t vprev, uint32_t v,
                                            uint32_t& maxg, uint32_t& maxgs) {
   const uint32_t g = v - vprev;
   const uint32_t bin = g >> 1;
-  if (bin < (uint32_t)kSmemBins) {
-    atomicAdd(sk.shist + bin, 1u);
-  } else {
-    atomicAdd(&sk.acc->hist[bin < (uint32_t)kHistBins ? bin : kHistBins - 1], 1ull);
-  }
-  if (g > maxg) { maxg = g; maxgs = vprev; }
-  if (g >= kLargeGap) {
-    const unsigned idx = atomicAdd(sk.n_large, 1u);
-    if (idx < sk.cap) {
-      LargeGapRec r; r.pos = sk.base + v; r.gap = g; r.req = sk.req;
-      sk.large[idx] = r;
+  atomicAdd(sk.shist + min(bin, (uint32_t)kSmemBins), 1u);
+  // rare: a new maximum, g >= kLargeGap, or g >= 2*kSmemBins (> kLargeGap)
+  if (g > min(maxg, kLargeGap - 1u)) {
+    if (g > maxg) { maxg = g; maxgs = vprev; }
+    if (bin >= (uint32_t)kSmemBins)
+      atomicAdd(&sk.acc->hist[bin < (uint32_t)kHistBins ? bin : kHistBins - 1], 1ull);
+    if (g >= kLargeGap) {
+      const unsigned idx = atomicAdd(sk.n_large, 1u);
+      if (idx < sk.cap) {
+        LargeGapRec r; r.pos = sk.base + v; r.gap = g; r.req = sk.req;
+        sk.large[idx] = r;
+      }
     }
   }
 }
@@ -103,7 +107,7 @@ sieve_segments_kernel(const SieveParams prm) {
   extern __shared__ __align__(16) uint32_t smem[];
   uint32_t* seg = smem;
   uint32_t* shist = seg + (prm.seg_bytes >> 2);
-  WarpRec* wrec = reinterpret_cast<WarpRec*>(shist + kSmemHistCopies * kSmemBins);
+  WarpRec* wrec = reinterpret_cast<WarpRec*>(shist + kSmemHistCopies * kSmemStride);
 
   __shared__ uint64_t s_k0, s_seg_in_req;
   __shared__ uint32_t s_req, s_nbytes, s_np, s_ctr;
@@ -112,7 +116,7 @@ sieve_segments_kernel(const SieveParams prm) {
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t nthr = blockDim.x, nwarps = nthr >> 5;
 
-  for (uint32_t i = tid; i < kSmemHistCopies * kSmemBins; i += nthr) shist[i] = 0;
+  for (uint32_t i = tid; i < kSmemHistCopies * kSmemStride; i += nthr) shist[i] = 0;
   if (tid < 32) s_vtab[tid] = 30u * (tid >> 3) + w30(tid & 7u);
   if (tid == 0) s_ctr = 0;
   int cur_req = -1;
@@ -151,7 +155,7 @@ sieve_segments_kernel(const SieveParams prm) {
         for (uint32_t bn = tid; bn < (uint32_t)kSmemBins; bn += nthr) {
           uint32_t s = 0;
 #pragma unroll
-          for (int c = 0; c < kSmemHistCopies; ++c) { s += shist[c * kSmemBins + bn]; shist[c * kSmemBins + bn] = 0; }
+          for (int c = 0; c < kSmemHistCopies; ++c) { s += shist[c * kSmemStride + bn]; shist[c * kSmemStride + bn] = 0; }
           if (s) atomicAdd(&prm.acc[cur_req].hist[bn], (unsigned long long)s);
         }
       }
@@ -175,8 +179,12 @@ sieve_segments_kernel(const SieveParams prm) {
     //      4, class o), eight rounds of four primes, loads of all rounds
     //      issued before any marking so their latency overlaps.
     {
+      // unit layout: [0, nsmall) small primes, then 32-prime units of the mid
+      // tier (split <= p < S), then 32-prime units of the huge tier (p >= S)
       const uint32_t nsmall = prm.tier_split < np ? prm.tier_split : np;
-      const uint32_t nunits = nsmall + (np - nsmall + 31u) / 32u;
+      const uint32_t hbeg = prm.tier_huge < np ? max(prm.tier_huge, nsmall) : np;
+      const uint32_t nmidu = (hbeg - nsmall + 31u) / 32u;
+      const uint32_t nunits = nsmall + nmidu + (np - hbeg + 31u) / 32u;
       const uint32_t o = lane & 7u, h = lane >> 3;
       for (;;) {
         uint32_t u = 0;
@@ -198,12 +206,31 @@ sieve_segments_kernel(const SieveParams prm) {
 #pragma unroll 4
             for (; w < lim; w += p) atomicAnd(seg + w, mask);
           }
+        } else if (u >= nsmall + nmidu) {
+          // huge tier: p >= S, at most one hit per class; a lane per prime,
+          // the eight classes unrolled, clears predicated (no loop).
+          const uint32_t i = hbeg + 32u * (u - nsmall - nmidu) + lane;
+          if (i < np) {
+            const uint32_t p = __ldg(prm.P + i);
+            const uint64_t mg = __ldg(prm.M + i);
+            uint32_t rr[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) rr[t] = __ldg(prm.R + t * prm.rstride + i);
+            const uint32_t m = mod_barrett(k0, p, mg);
+            const bool low = 30ull * k0 < (uint64_t)p * p;
+#pragma unroll
+            for (uint32_t t = 0; t < 8; ++t) {
+              uint32_t s = rr[t] >= m ? rr[t] - m : rr[t] + p - m;
+              if (low) s = lift_to_square(s, k0, p, t, nbytes);
+              if (s < nbytes) clear_bit(seg, s, t);
+            }
+          }
         } else {
-          // p and k0 mod p once per prime (lane = prime), then shuffled to the
-          // (prime, class) lanes of each round.
+          // mid tier: p and k0 mod p once per prime (lane = prime), then
+          // shuffled to the (prime, class) lanes of each round.
           const uint32_t base = nsmall + 32u * (u - nsmall);
           const uint32_t im = base + lane;
-          const bool okm = im < np;
+          const bool okm = im < hbeg;
           const uint32_t pm = okm ? __ldg(prm.P + im) : 0u;
           const uint32_t mm = okm ? mod_barrett(k0, pm, __ldg(prm.M + im)) : 0u;
           const bool low_any = __any_sync(0xFFFFFFFFu, okm && 30ull * k0 < (uint64_t)pm * pm);
@@ -211,7 +238,7 @@ sieve_segments_kernel(const SieveParams prm) {
 #pragma unroll
           for (int t = 0; t < 8; ++t) {
             const uint32_t i = base + 4u * t + h;
-            rr[t] = i < np ? __ldg(prm.R + o * prm.rstride + i) : 0u;
+            rr[t] = i < hbeg ? __ldg(prm.R + o * prm.rstride + i) : 0u;
           }
 #pragma unroll
           for (int t = 0; t < 8; ++t) {
@@ -220,7 +247,22 @@ sieve_segments_kernel(const SieveParams prm) {
             if (!p) continue;
             uint32_t s = rr[t] >= m ? rr[t] - m : rr[t] + p - m;
             if (low_any && 30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
-            for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, o);
+            if (4u * p <= nbytes) {
+              // >= 4 hits: four streams of step 4p bytes = p words, each with
+              // a fixed bit mask
+#pragma unroll
+              for (uint32_t k = 0; k < 4; ++k) {
+                const uint32_t jk = s + k * p;
+                if (jk < nbytes) {
+                  const uint32_t c = jk & 3u;
+                  const uint32_t mask = ~(1u << ((c << 3) | o));
+                  const uint32_t lim = (nbytes - c + 3u) >> 2;
+                  for (uint32_t w = jk >> 2; w < lim; w += p) atomicAnd(seg + w, mask);
+                }
+              }
+            } else {
+              for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, o);
+            }
           }
         }
       }
@@ -260,7 +302,7 @@ sieve_segments_kernel(const SieveParams prm) {
     //    stitched with a warp max-scan of their last prime, warps by thread 0.
     {
       GapSink sk;
-      sk.shist = shist + (warp % kSmemHistCopies) * kSmemBins;
+      sk.shist = shist + (warp % kSmemHistCopies) * kSmemStride;
       sk.acc = prm.acc + req;
       sk.large = prm.large; sk.n_large = prm.n_large; sk.cap = prm.large_cap;
       sk.req = req; sk.base = 30ull * k0;
@@ -276,14 +318,25 @@ sieve_segments_kernel(const SieveParams prm) {
         c41 += __popc(w & m41);
         c31 += __popc(w & 0x2B2B2B2Bu);
         const uint32_t vb = 120u * wi;
-        do {
+        if (!last1) {                       // the run's first prime opens no gap
           const uint32_t bp = (uint32_t)__ffs(w) - 1u;
           w &= w - 1u;
-          const uint32_t v = vb + s_vtab[bp];
-          if (last1) record_gap(sk, last1 - 1u, v, maxg, maxgs);
-          else first1 = v + 1u;
-          last1 = v + 1u;
-        } while (w);
+          first1 = last1 = vb + s_vtab[bp] + 1u;
+        }
+        // two primes per step: their lookups are independent, so their
+        // latencies overlap
+        while (w) {
+          const uint32_t bp1 = (uint32_t)__ffs(w) - 1u;
+          w &= w - 1u;
+          const bool two = w != 0;
+          const uint32_t bp2 = ((uint32_t)__ffs(w) - 1u) & 31u;
+          w &= w - 1u;
+          const uint32_t v1 = vb + s_vtab[bp1];
+          const uint32_t v2 = vb + s_vtab[bp2];
+          record_gap(sk, last1 - 1u, v1, maxg, maxgs);
+          if (two) record_gap(sk, v1, v2, maxg, maxgs);
+          last1 = (two ? v2 : v1) + 1u;
+        }
       }
       // lane stitching: previous lane's last prime (values grow with the lane)
       uint32_t sc = last1;
@@ -342,7 +395,7 @@ sieve_segments_kernel(const SieveParams prm) {
     for (uint32_t bn = tid; bn < (uint32_t)kSmemBins; bn += nthr) {
       uint32_t s = 0;
 #pragma unroll
-      for (int c = 0; c < kSmemHistCopies; ++c) s += shist[c * kSmemBins + bn];
+      for (int c = 0; c < kSmemHistCopies; ++c) s += shist[c * kSmemStride + bn];
       if (s) atomicAdd(&prm.acc[cur_req].hist[bn], (unsigned long long)s);
     }
   }
@@ -431,7 +484,7 @@ finalize_kernel(const ReqDesc* __restrict__ reqs, const SegRec* __restrict__ seg
 // host-side launchers (called by the engine)
 // ---------------------------------------------------------------------------
 size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads) {
-  return (size_t)seg_bytes + sizeof(uint32_t) * kSmemHistCopies * kSmemBins +
+  return (size_t)seg_bytes + sizeof(uint32_t) * kSmemHistCopies * kSmemStride +
          sizeof(WarpRec) * (threads / 32);
 }
 

@@ -14,7 +14,8 @@ namespace vg {
 constexpr uint64_t kW30Packed = 0x1D1713110D0B0701ull;  // W30[o] = byte o
 constexpr int kHistBins = 1025;       // gap/2 bins 0..1023, bin 1024 = gap >= 2048
 constexpr int kSmemBins = 256;        // bins kept in shared memory (gap < 512)
-constexpr int kSmemHistCopies = 16;   // one copy per 2 warps
+constexpr int kSmemHistCopies = 8;    // one copy per 4 warps
+constexpr int kSmemStride = kSmemBins + 4;   // + the overflow bin, padded
 constexpr uint32_t kLargeGap = 500;   // the reference's large-gap threshold
 constexpr uint32_t kTileAPeriod = 7u * 11u * 13u * 17u;      // 17017 bytes
 constexpr uint32_t kTileBPeriod = 19u * 23u * 29u * 31u;     // 392863 bytes
@@ -78,7 +79,8 @@ struct SieveParams {
   const uint32_t* tileA;     // presieve tiles, extended past their period
   const uint32_t* tileB;
   uint32_t seg_bytes;        // S, a multiple of 128
-  uint32_t tier_split;       // table index of the first thread-per-prime prime
+  uint32_t tier_split;       // table index of the first mid-tier prime
+  uint32_t tier_huge;        // table index of the first prime >= seg_bytes
   SegRec* segs;
   ReqAccum* acc;
   LargeGapRec* large;
