@@ -248,6 +248,7 @@ def test_configs_agree(vg, oracle_lib):
         cases = [(0, 3 * 10**8), (10**12, 10**12 + 10**8), (987654321, 987654321 + 5 * 10**7)]
         want = [oracle_lib.range_stats(a, b) for a, b in cases]
         for cfg in (dict(seg_bytes=65536, threads=512, tier_split=1024, auto_tune=0),
+                    dict(seg_bytes=221184, threads=1024, tier_split=2048, auto_tune=0),
                     dict(seg_bytes=196608, threads=1024, tier_split=4096, auto_tune=0),
                     dict(seg_bytes=32768, threads=256, tier_split=37, auto_tune=0),
                     dict(seg_bytes=131072, threads=768, tier_split=100000, ctas_per_sm=1, auto_tune=0)):

@@ -247,22 +247,7 @@ sieve_segments_kernel(const SieveParams prm) {
             if (!p) continue;
             uint32_t s = rr[t] >= m ? rr[t] - m : rr[t] + p - m;
             if (low_any && 30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
-            if (4u * p <= nbytes) {
-              // >= 4 hits: four streams of step 4p bytes = p words, each with
-              // a fixed bit mask
-#pragma unroll
-              for (uint32_t k = 0; k < 4; ++k) {
-                const uint32_t jk = s + k * p;
-                if (jk < nbytes) {
-                  const uint32_t c = jk & 3u;
-                  const uint32_t mask = ~(1u << ((c << 3) | o));
-                  const uint32_t lim = (nbytes - c + 3u) >> 2;
-                  for (uint32_t w = jk >> 2; w < lim; w += p) atomicAnd(seg + w, mask);
-                }
-              }
-            } else {
-              for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, o);
-            }
+            for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, o);
           }
         }
       }
@@ -318,25 +303,14 @@ sieve_segments_kernel(const SieveParams prm) {
         c41 += __popc(w & m41);
         c31 += __popc(w & 0x2B2B2B2Bu);
         const uint32_t vb = 120u * wi;
-        if (!last1) {                       // the run's first prime opens no gap
+        do {
           const uint32_t bp = (uint32_t)__ffs(w) - 1u;
           w &= w - 1u;
-          first1 = last1 = vb + s_vtab[bp] + 1u;
-        }
-        // two primes per step: their lookups are independent, so their
-        // latencies overlap
-        while (w) {
-          const uint32_t bp1 = (uint32_t)__ffs(w) - 1u;
-          w &= w - 1u;
-          const bool two = w != 0;
-          const uint32_t bp2 = ((uint32_t)__ffs(w) - 1u) & 31u;
-          w &= w - 1u;
-          const uint32_t v1 = vb + s_vtab[bp1];
-          const uint32_t v2 = vb + s_vtab[bp2];
-          record_gap(sk, last1 - 1u, v1, maxg, maxgs);
-          if (two) record_gap(sk, v1, v2, maxg, maxgs);
-          last1 = (two ? v2 : v1) + 1u;
-        }
+          const uint32_t v = vb + s_vtab[bp];
+          if (last1) record_gap(sk, last1 - 1u, v, maxg, maxgs);
+          else first1 = v + 1u;
+          last1 = v + 1u;
+        } while (w);
       }
       // lane stitching: previous lane's last prime (values grow with the lane)
       uint32_t sc = last1;
