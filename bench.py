@@ -223,7 +223,40 @@ def secondary(torch, stream, flush):
                                              "max_minp": res["max"], "counterexamples": res["counterexamples"],
                                              "probes": res["probes"]}
     g.close()
+    out["C5 serving mix"] = serving(torch)
     return out
+
+
+def serving(torch, n=2000):
+    """Served (continuous batching) vs plain one-call-per-request, same stream."""
+    from voss_gb300.serve import Server, run_plain, run_served, same_answer, serving_mix
+    reqs = serving_mix(n)
+    warm = serving_mix(64, seed=1)
+    run_plain(warm)
+    plain, plain_s = run_plain(reqs)
+    with Server() as srv:
+        run_served(srv, warm)
+        srv.reset_metrics()
+        res, lat, wall = run_served(srv, reqs)
+        m_sat = srv.metrics()
+        rate = 0.7 * n / wall
+        srv.reset_metrics()
+        res2, lat2, wall2 = run_served(srv, reqs, rate=rate, seed=3)
+        m_rate = srv.metrics()
+    ok = all(same_answer(r, x, y) for r, x, y in zip(reqs, res, plain)) and \
+        all(same_answer(r, x, y) for r, x, y in zip(reqs, res2, plain))
+    ints = sum(r.b - r.a for r in reqs)
+    lat_s, lat_r = sorted(lat), sorted(lat2)
+    q = lambda v, f: v[min(len(v) - 1, int(f * (len(v) - 1) + 0.5))]
+    return {"requests": n, "integers": ints, "all_results_equal_plain": ok,
+            "plain_req_per_s": n / plain_s, "plain_s": plain_s,
+            "served_req_per_s": n / wall, "served_s": wall,
+            "speedup_req_per_s": plain_s / wall,
+            "served_p50_ms": q(lat_s, 0.5) / 1e3, "served_p99_ms": q(lat_s, 0.99) / 1e3,
+            "batches": m_sat["batches"], "mean_batch": m_sat["mean_batch"],
+            "max_inflight_batches": m_sat["max_inflight_batches"],
+            "poisson_rate_req_per_s": rate, "poisson_req_per_s": n / wall2,
+            "poisson_p50_ms": q(lat_r, 0.5) / 1e3, "poisson_p99_ms": q(lat_r, 0.99) / 1e3}
 
 
 def run_ours(args, rank, world, local_rank):

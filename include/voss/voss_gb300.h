@@ -119,6 +119,51 @@ int voss_gb300_goldbach_results(voss_gb300_goldbach* g, uint32_t* max_minp,
                                 uint64_t* hist, uint64_t* probes, void* stream);
 void voss_gb300_goldbach_free(voss_gb300_goldbach* g);
 
+/* Request server with continuous batching.  Requests (a range and what is
+ * asked of it) are submitted at any time; a scheduler thread packs the
+ * pending ones into batches, FIFO, while batch slots and device memory
+ * (segment records, accumulators, results of every batch in flight) allow,
+ * and runs each batch as one replayed CUDA graph on its slot's stream, so
+ * batches overlap on the device.  The reference has no counterpart: it
+ * serves one Context at a time (context.cu:212-559).  Every request gets the
+ * full voss_range_stats_t; for COUNT and CHEBYSHEV requests the gap fields
+ * are not computed (zero). */
+#define VOSS_OP_COUNT      0
+#define VOSS_OP_TWINS      1
+#define VOSS_OP_GAP_HIST   2
+#define VOSS_OP_CHEBYSHEV  3
+
+typedef struct {
+    uint32_t slots;               /* batches in flight (default 4) */
+    uint32_t max_batch;           /* requests per batch (default 256) */
+    uint64_t max_segments;        /* segments per batch (default 32768) */
+    uint64_t memory_budget;       /* device bytes over all batches in flight */
+    uint32_t use_graphs;          /* replay a captured CUDA graph per batch */
+} voss_gb300_server_config_t;
+
+typedef struct {
+    uint64_t submitted, completed, pending, batches;
+    uint64_t max_inflight_batches, peak_admitted_bytes;
+    double p50_us, p99_us, mean_us;   /* submit -> result ready */
+    double req_per_s;                 /* completed / (last completion - first submit) */
+    double mean_batch;
+} voss_gb300_server_metrics_t;
+
+typedef struct voss_gb300_server voss_gb300_server;
+
+/* cfg may be NULL (defaults); zero fields take the defaults. */
+int voss_gb300_server_create(const voss_gb300_server_config_t* cfg, voss_gb300_server** out);
+int voss_gb300_server_submit(voss_gb300_server* s, uint64_t a, uint64_t b, uint32_t op,
+                             uint64_t* ticket);
+/* wait = 0: *ready = 0 if the result is not there yet.  On ready, *out gets
+ * the result and the ticket is released. */
+int voss_gb300_server_result(voss_gb300_server* s, uint64_t ticket, int wait,
+                             voss_range_stats_t* out, double* latency_us, int* ready);
+int voss_gb300_server_drain(voss_gb300_server* s);
+int voss_gb300_server_metrics(voss_gb300_server* s, voss_gb300_server_metrics_t* out);
+int voss_gb300_server_reset_metrics(voss_gb300_server* s);
+void voss_gb300_server_free(voss_gb300_server* s);
+
 /* Shared-memory bandwidth of this GPU in GB/s, measured by two
  * microbenchmarks (conflict-free 32-bit load+store, and atomicAnd; 8 bytes
  * per step each): the denominators of the sieve's roofline. */

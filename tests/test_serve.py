@@ -1,0 +1,72 @@
+"""The request server: continuous batching gives each request the same answer
+it gets alone, under load, with overlapping batches; admission respects its
+limits; CPU-side pieces (the request generator) need no GPU."""
+import numpy as np
+import pytest
+
+
+def test_serving_mix_generator_is_seeded_and_shaped():
+    from conftest import build_library
+    build_library()
+    from voss_gb300.serve import OP_COUNT, serving_mix
+    a = serving_mix(2000, seed=5)
+    b = serving_mix(2000, seed=5)
+    assert [(r.a, r.b, r.op) for r in a] == [(r.a, r.b, r.op) for r in b]
+    w = np.array([r.b - r.a for r in a], dtype=np.float64)
+    s = np.array([r.a for r in a], dtype=np.float64)
+    assert w.min() >= 1e3 and w.max() <= 1e10 and s.min() >= 0 and s.max() < 1e13
+    ops = np.array([r.op for r in a])
+    assert 0.45 < (ops == OP_COUNT).mean() < 0.55
+
+
+@pytest.mark.gpu
+def test_served_equals_alone(vg, oracle_lib):
+    from voss_gb300.serve import GAP_OPS, Server, run_served, same_answer, serving_mix
+    reqs = serving_mix(400, seed=99, max_start=1e12)
+    reqs = [r for r in reqs if r.b - r.a <= 3 * 10**8]          # keep the alone runs quick
+    with Server(slots=3, max_batch=32) as srv:
+        res, lat, wall = run_served(srv, reqs)
+        m = srv.metrics()
+    assert m["completed"] == len(reqs) and m["batches"] >= 2
+    assert m["max_inflight_batches"] >= 2          # batches overlapped on the device
+    for r, got in zip(reqs, res):
+        alone = vg.range_stats(r.a, r.b)
+        assert same_answer(r, got, alone), (r, got, alone)
+    for r, got in list(zip(reqs, res))[:40]:
+        orc = oracle_lib.range_stats(r.a, r.b)
+        assert got.count == orc["count"]
+        if r.op in GAP_OPS:
+            assert got.max_gap == orc["max_gap"] and got.twins == int(orc["hist"][1])
+
+
+@pytest.mark.gpu
+def test_poisson_arrivals_and_admission_limits(vg):
+    from voss_gb300.serve import Server, run_served, same_answer, serving_mix
+    reqs = serving_mix(300, seed=7, max_start=1e11)
+    reqs = [r for r in reqs if r.b - r.a <= 10**8]
+    # a tight memory budget forces small batches; graphs off exercises the
+    # plain launch path of a slot
+    with Server(slots=2, max_batch=8, memory_budget=200_000, use_graphs=False) as srv:
+        res, lat, wall = run_served(srv, reqs, rate=2000.0)
+        m = srv.metrics()
+    assert m["completed"] == len(reqs)
+    assert m["mean_batch"] <= 8.0
+    assert m["peak_admitted_bytes"] <= 200_000 or m["mean_batch"] == 1.0
+    for r, got in zip(reqs[:100], res[:100]):
+        assert same_answer(r, got, vg.range_stats(r.a, r.b))
+    assert m["p99_us"] >= m["p50_us"] > 0
+
+
+@pytest.mark.gpu
+def test_server_rejects_oversized_and_bad_ops(vg):
+    from voss_gb300.serve import Server
+    with Server(slots=1, max_segments=64) as srv:
+        with pytest.raises(vg.VossError):
+            srv.submit(0, 10**11)                  # needs more than 64 segments
+        with pytest.raises(vg.VossError):
+            srv.submit(0, 1000, 9)
+        t = srv.submit(0, 1000, 0)
+        got, lat = srv.result(t)
+        assert got.count == 168
+        with pytest.raises(vg.VossError):
+            srv.result(t)                          # already collected

@@ -21,7 +21,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libvoss.so"
-SOURCES = ["sieve.cu", "goldbach.cu", "probe.cu", "engine.cpp", "capi.cpp"]
+SOURCES = ["sieve.cu", "goldbach.cu", "probe.cu", "engine.cpp", "serve.cpp", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -70,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB.with_name("libvoss.so.tmp%d" % os.getpid())
-    link = [cc, *ARCH, "-shared", "-cudart", "shared", "-o", str(tmp), *map(str, objs),
+    link = [cc, *ARCH, "-shared", "-cudart", "shared", "-o", str(tmp), *map(str, objs), "-lpthread",
             "-Xlinker", "-rpath," + cuda_lib_dir()]
     if verbose:
         print(" ".join(link), flush=True)

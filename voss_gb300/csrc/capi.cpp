@@ -16,6 +16,7 @@
 
 #include "engine.h"
 #include "goldbach.h"
+#include "serve.h"
 #include "voss/voss.h"
 #include "voss/voss_gb300.h"
 #include "voss/voss_numbers.h"
@@ -156,7 +157,7 @@ void compute_ctx(voss_primes_ctx* c) {
   if (!c->cb) {
     std::vector<vg::LargeGapRec> lg;
     uint64_t a = 0, b = N + 1;
-    const vg::ReqResult* r = E.run(1, &a, &b, gaps ? &lg : nullptr);
+    const vg::ReqResult* r = E.run(1, &a, &b, gaps ? &lg : nullptr, gaps);
     merge_into(m, r[0], lg, 0);
   } else {
     uint64_t cumulative = 3;
@@ -165,7 +166,7 @@ void compute_ctx(voss_primes_ctx* c) {
       const uint64_t hi = std::min<uint64_t>((s + 1) * segn, N);
       std::vector<vg::LargeGapRec> lg;
       uint64_t a = lo, b = hi + 1;
-      const vg::ReqResult* r = E.run(1, &a, &b, gaps ? &lg : nullptr);
+      const vg::ReqResult* r = E.run(1, &a, &b, gaps ? &lg : nullptr, gaps);
       vg::ReqResult copy = r[0];
       merge_into(m, copy, lg, 0);
       // primes >= 7 in the chunk (the reference's n_pos, context.cu:423-436)
@@ -426,7 +427,7 @@ extern "C" int voss_primes_prime_count(uint64_t N, uint64_t* out) {
     vg::Engine& E = vg::Engine::for_current_device();
     std::lock_guard<std::mutex> g(E.mu);
     uint64_t a = 0, b = N + 1;
-    *out = E.run(1, &a, &b)[0].count;
+    *out = E.run(1, &a, &b, nullptr, false)[0].count;
     return VOSS_OK;
   }, VOSS_ERR_CUDA);
 }
@@ -643,7 +644,7 @@ extern "C" int voss_gb300_plan_info(voss_gb300_plan* p, uint64_t* total_segments
     if (total_segments) *total_segments = p->plan.total_segs;
     if (grid) *grid = p->plan.grid;
     if (kernels_per_run) *kernels_per_run = p->plan.nreq ? vg::Plan::kKernels : 0;
-    if (smem_bytes) *smem_bytes = (uint32_t)vg::sieve_smem_bytes(p->plan.cfg.seg_bytes, p->plan.cfg.threads);
+    if (smem_bytes) *smem_bytes = (uint32_t)vg::sieve_smem_bytes(p->plan.seg_max, p->plan.threads);
     if (clears) *clears = p->plan.algorithmic_clears();
     if (wheel_bytes) *wheel_bytes = p->plan.wheel_bytes();
     return VOSS_OK;
@@ -743,3 +744,68 @@ extern "C" int voss_gb300_goldbach_results(voss_gb300_goldbach* h, uint32_t* max
 }
 
 extern "C" void voss_gb300_goldbach_free(voss_gb300_goldbach* h) { delete h; }
+
+// ---------------------------------------------------------------------------
+// Request server
+// ---------------------------------------------------------------------------
+struct voss_gb300_server {
+  std::unique_ptr<vg::Server> s;
+};
+
+extern "C" int voss_gb300_server_create(const voss_gb300_server_config_t* c, voss_gb300_server** out) {
+  if (!out) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+  *out = nullptr;
+  return guarded([&] {
+    vg::ServerConfig sc;
+    if (c) {
+      if (c->slots) sc.slots = c->slots;
+      if (c->max_batch) sc.max_batch = c->max_batch;
+      if (c->max_segments) sc.max_segs = c->max_segments;
+      if (c->memory_budget) sc.mem_budget = c->memory_budget;
+      sc.use_graphs = c->use_graphs;
+    }
+    vg::Engine& E = vg::Engine::for_current_device();
+    auto* h = new voss_gb300_server();
+    try {
+      h->s.reset(new vg::Server(E, sc));
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+    return VOSS_OK;
+  }, VOSS_ERR_INTERNAL);
+}
+
+extern "C" int voss_gb300_server_submit(voss_gb300_server* h, uint64_t a, uint64_t b, uint32_t op,
+                                        uint64_t* ticket) {
+  if (!h || !ticket) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+  return guarded([&] { *ticket = h->s->submit(a, b, op); return VOSS_OK; }, VOSS_ERR_INTERNAL);
+}
+
+extern "C" int voss_gb300_server_result(voss_gb300_server* h, uint64_t ticket, int wait,
+                                        voss_range_stats_t* out, double* latency_us, int* ready) {
+  if (!h) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+  return guarded([&] {
+    const bool ok = h->s->result(ticket, wait != 0, out, latency_us);
+    if (ready) *ready = ok ? 1 : 0;
+    return VOSS_OK;
+  }, VOSS_ERR_INTERNAL);
+}
+
+extern "C" int voss_gb300_server_drain(voss_gb300_server* h) {
+  if (!h) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+  return guarded([&] { h->s->drain(); return VOSS_OK; }, VOSS_ERR_INTERNAL);
+}
+
+extern "C" int voss_gb300_server_metrics(voss_gb300_server* h, voss_gb300_server_metrics_t* out) {
+  if (!h || !out) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+  return guarded([&] { h->s->metrics(out); return VOSS_OK; }, VOSS_ERR_INTERNAL);
+}
+
+extern "C" int voss_gb300_server_reset_metrics(voss_gb300_server* h) {
+  if (!h) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+  return guarded([&] { h->s->reset_metrics(); return VOSS_OK; }, VOSS_ERR_INTERNAL);
+}
+
+extern "C" void voss_gb300_server_free(voss_gb300_server* h) { delete h; }

@@ -190,79 +190,202 @@ uint32_t Engine::index_of(uint32_t p) const {
   return (uint32_t)(std::lower_bound(hP.begin(), hP.end(), p) - hP.begin());
 }
 
-Config Engine::tuned_for(uint64_t a, uint64_t b) const {
+Config Engine::tuned_for(uint64_t a, uint64_t b, bool batch) const {
   Config c = cfg;
   if (!cfg.auto_tune) return c;
-  // Offset regimes: for small ranges a smaller segment spreads the work over
-  // more SMs; the split between the warp-per-prime tier and the
-  // four-primes-per-warp tier sits where a class has about 32 hits per
-  // segment (measured best on GB300 for 1e10..1e14).
   const uint64_t width = b > a ? b - a : 0;
   const uint64_t bytes = width / 30 + 1;
+  for (const TuneEntry& t : tuning) {
+    if (b <= t.b_max && width <= t.width_max) {
+      c.seg_bytes = std::min<uint32_t>(std::max<uint32_t>(t.seg_bytes, 1024), cfg.seg_bytes) & ~127u;
+      c.tier_split = std::max<uint32_t>(kFirstTablePrime, t.tier_split);
+      return c;
+    }
+  }
+  // Built-in rule.  Alone, a range should fill the GPU in whole waves: the
+  // segment is shrunk until the segments come in full waves of one CTA per
+  // SM (not below 16 KiB, where the per-prime setup dominates).  In a batch
+  // other ranges fill the GPU, so the largest segment is the cheapest.
   uint32_t s = cfg.seg_bytes;
-  const uint64_t want_segs = (uint64_t)sm_count * cfg.ctas_per_sm;
-  while (s > 16384 && bytes / s < want_segs) s /= 2;
-  c.seg_bytes = (s + 127) & ~127u;
-  c.tier_split = std::max<uint32_t>(kFirstTablePrime, c.seg_bytes / 32);
+  if (!batch) {
+    const uint64_t g = (uint64_t)sm_count * cfg.ctas_per_sm;
+    const uint64_t waves = (bytes + g * s - 1) / (g * s);
+    uint64_t want = (bytes + waves * g - 1) / (waves * g);
+    want = std::max<uint64_t>(want, 16384);
+    s = (uint32_t)std::min<uint64_t>(s, (want + 127) & ~127ull);
+  }
+  c.seg_bytes = s;
+  // The warp-per-prime tier ends where a class has about 32 hits per
+  // segment (measured best on GB300 between 1e10 and 1e14).
+  c.tier_split = std::max<uint32_t>(kFirstTablePrime, std::min<uint32_t>(cfg.tier_split, s / 32));
   return c;
 }
 
 // ---------------------------------------------------------------------------
 // Plan
 // ---------------------------------------------------------------------------
-void Plan::prepare(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl) {
+void Plan::reserve_capacity(uint32_t max_req, uint64_t max_segs) {
+  cap_req = std::max<uint32_t>(max_req, 1);
+  cap_segs = std::max<uint64_t>(max_segs, 1);
+  reqs.reserve(sizeof(ReqDesc) * cap_req);
+  segs.reserve(sizeof(SegRec) * cap_segs);
+  acc.reserve(sizeof(ReqAccum) * cap_req);
+  results.reserve(sizeof(ReqResult) * cap_req);
+  stage.reserve(sizeof(BatchHdr) + sizeof(ReqDesc) * cap_req);
+  host_results.reserve(sizeof(ReqResult) * cap_req);
+}
+
+uint64_t Plan::segments_for(uint64_t a, uint64_t b) const {
+  if (b <= a) return 0;
+  const Config c = eng->tuned_for(a, b, batch_mode);
+  const uint64_t bytes = (b + 29) / 30 - a / 30;
+  return (bytes + c.seg_bytes - 1) / c.seg_bytes;
+}
+
+void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
+                const uint32_t* rflags) {
   Engine& E = *eng;
   flags = fl;
-  nreq = n;
-  uint64_t max_b = 0, min_a = UINT64_MAX;
+  uint64_t max_b = 0;
   for (uint32_t i = 0; i < n; ++i) {
     if (b[i] > kMaxB) throw Error(VOSS_ERR_OUT_OF_RANGE, "range end exceeds 10^14 + 10^10 + 1");
-    if (b[i] > a[i]) { max_b = std::max(max_b, b[i]); min_a = std::min(min_a, a[i]); }
+    if (b[i] > a[i]) max_b = std::max(max_b, b[i]);
   }
-  cfg = (n == 1 && max_b) ? E.tuned_for(a[0], b[0]) : E.cfg;
-  if (!E.cfg.auto_tune) cfg = E.cfg;
+  if (cap_req && n > cap_req) throw Error(VOSS_ERR_INVALID_ARG, "batch exceeds the plan's capacity");
   if (max_b > 1) E.ensure_table(isqrt_u64(max_b - 1));
-  tier_split_idx = E.index_of(cfg.tier_split);
-  tier_huge_idx = E.index_of(cfg.seg_bytes);
+  threads = E.cfg.threads;
+  const bool many = n > 1 || batch_mode;
 
-  host_reqs.assign(n, ReqDesc{});
-  uint64_t segs_total = 0;
+  struct Item { ReqDesc d; double cost; uint32_t idx; };
+  std::vector<Item> items(n);
+  uint32_t smax = 0;
   for (uint32_t i = 0; i < n; ++i) {
-    ReqDesc& r = host_reqs[i];
+    ReqDesc r{};
     r.a = a[i];
     r.b = b[i];
-    r.seg_base = segs_total;
+    r.rflags = rflags ? rflags[i] : kReqGaps;
+    double cost = 0;
     if (b[i] > a[i]) {
+      const Config c = E.tuned_for(a[i], b[i], many);
       r.k_lo = a[i] / 30;
       r.k_hi = (b[i] + 29) / 30;
-      r.nseg = (r.k_hi - r.k_lo + cfg.seg_bytes - 1) / cfg.seg_bytes;
+      r.seg_bytes = c.seg_bytes;
+      r.nseg = (r.k_hi - r.k_lo + c.seg_bytes - 1) / c.seg_bytes;
       r.nprimes = E.primes_below_sq(b[i]);
+      r.tier_split = E.index_of(c.tier_split);
+      r.tier_huge = E.index_of(c.seg_bytes);
+      smax = std::max(smax, c.seg_bytes);
+      // per segment: fill and scan grow with the bytes, setup with the primes
+      cost = (double)r.nseg * ((double)c.seg_bytes + 24.0 * r.nprimes);
+    } else {
+      r.seg_bytes = 128;
     }
-    segs_total += r.nseg;
+    items[i] = Item{r, cost, i};
   }
-  total_segs = segs_total;
+  if (n > 1)
+    std::stable_sort(items.begin(), items.end(),
+                     [](const Item& x, const Item& y) { return x.cost > y.cost; });
+  host_reqs.resize(n);
+  order.resize(n);
+  uint64_t base = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    host_reqs[i] = items[i].d;
+    host_reqs[i].seg_base = base;
+    order[i] = items[i].idx;
+    base += host_reqs[i].nseg;
+  }
+  nreq = n;
+  total_segs = base;
+  if (cap_req) {
+    if (total_segs > cap_segs) throw Error(VOSS_ERR_INVALID_ARG, "batch exceeds the plan's segment capacity");
+    seg_max = E.cfg.seg_bytes;     // fixed for graph replay
+  } else {
+    seg_max = std::max<uint32_t>(smax, 128);
+    reqs.reserve(sizeof(ReqDesc) * std::max<uint32_t>(n, 1));
+    segs.reserve(sizeof(SegRec) * std::max<uint64_t>(total_segs, 1));
+    acc.reserve(sizeof(ReqAccum) * std::max<uint32_t>(n, 1));
+    results.reserve(sizeof(ReqResult) * std::max<uint32_t>(n, 1));
+    stage.reserve(sizeof(BatchHdr) + sizeof(ReqDesc) * std::max<uint32_t>(n, 1));
+    host_results.reserve(sizeof(ReqResult) * std::max<uint32_t>(n, 1));
+  }
   if (flags & kFlagBitmap) {
     if (n != 1) throw Error(VOSS_ERR_INTERNAL, "bitmap output needs exactly one range");
     const uint64_t words = (host_reqs[0].k_hi - host_reqs[0].k_lo + 3) / 4 + 1;
     bitmap.reserve(words * 4);
   }
-  reqs.reserve(sizeof(ReqDesc) * std::max<uint32_t>(n, 1));
-  segs.reserve(sizeof(SegRec) * std::max<uint64_t>(total_segs, 1));
-  acc.reserve(sizeof(ReqAccum) * std::max<uint32_t>(n, 1));
-  results.reserve(sizeof(ReqResult) * std::max<uint32_t>(n, 1));
+  hdr.reserve(sizeof(BatchHdr));
+  queue.reserve(sizeof(unsigned long long));
   large.reserve(sizeof(LargeGapRec) * large_cap);
   nlarge.reserve(sizeof(unsigned int));
-  if (n)
-    check_cuda(cudaMemcpyAsync(reqs.ptr, host_reqs.data(), sizeof(ReqDesc) * n,
-                               cudaMemcpyHostToDevice, E.stream), "upload requests");
-  check_cuda(cudaStreamSynchronize(E.stream), "cudaStreamSynchronize(prepare)");
-  const uint64_t cap = (uint64_t)E.sm_count * cfg.ctas_per_sm;
-  grid = (uint32_t)std::min<uint64_t>(total_segs, cap);
+  BatchHdr* h = static_cast<BatchHdr*>(stage.ptr);
+  h->total_segs = total_segs;
+  h->nreq = nreq;
+  h->pad = 0;
+  if (n) std::memcpy(h + 1, host_reqs.data(), sizeof(ReqDesc) * n);
+  const uint64_t gcap = (uint64_t)E.sm_count * E.cfg.ctas_per_sm;
+  grid = (uint32_t)(cap_req ? gcap : std::min<uint64_t>(total_segs, gcap));
+
+  prm.reqs = reqs.as<ReqDesc>();
+  prm.hdr = hdr.as<BatchHdr>();
+  prm.queue = queue.as<unsigned long long>();
+  prm.P = E.dP.as<uint32_t>();
+  prm.M = E.dM.as<uint64_t>();
+  prm.R = E.dR.as<uint32_t>();
+  prm.rstride = E.rstride;
+  prm.tileA = E.tileA.as<uint32_t>();
+  prm.tileB = E.tileB.as<uint32_t>();
+  prm.seg_bytes = seg_max;
+  prm.segs = segs.as<SegRec>();
+  prm.acc = acc.as<ReqAccum>();
+  prm.large = large.as<LargeGapRec>();
+  prm.n_large = nlarge.as<unsigned int>();
+  prm.large_cap = large_cap;
+  prm.flags = flags;
+  prm.bitmap = bitmap.as<uint32_t>();
+}
+
+void Plan::prepare(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl) {
+  load(n, a, b, fl);
+}
+
+void Plan::upload(cudaStream_t s) {
+  const size_t bytes = sizeof(BatchHdr) + sizeof(ReqDesc) * nreq;
+  check_cuda(cudaMemcpyAsync(hdr.ptr, stage.ptr, sizeof(BatchHdr), cudaMemcpyHostToDevice, s),
+             "upload batch header");
+  if (nreq)
+    check_cuda(cudaMemcpyAsync(reqs.ptr, static_cast<const char*>(stage.ptr) + sizeof(BatchHdr),
+                               bytes - sizeof(BatchHdr), cudaMemcpyHostToDevice, s),
+               "upload requests");
 }
 
 Plan::~Plan() {
   for (cudaEvent_t& e : ev)
     if (e) cudaEventDestroy(e);
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  if (graph) cudaGraphDestroy(graph);
+}
+
+void Plan::capture(cudaStream_t s) {
+  if (!cap_req) throw Error(VOSS_ERR_INTERNAL, "graph capture needs a fixed-capacity plan");
+  if (graph_exec) return;
+  // the kernels' attributes are raised outside the capture
+  check_cuda(launch_sieve(prm, 0, threads, s), "sieve attributes");
+  check_cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+  try {
+    run_device(s);
+  } catch (...) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(s, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  check_cuda(cudaStreamEndCapture(s, &graph), "end capture");
+  check_cuda(cudaGraphInstantiate(&graph_exec, graph, 0), "graph instantiate");
+}
+
+void Plan::launch_graph(cudaStream_t s) {
+  if (!graph_exec) capture(s);
+  check_cuda(cudaGraphLaunch(graph_exec, s), "graph launch");
 }
 
 void Plan::kernel_ms(float* sieve_ms, float* finalize_ms) {
@@ -272,49 +395,41 @@ void Plan::kernel_ms(float* sieve_ms, float* finalize_ms) {
   if (finalize_ms) check_cuda(cudaEventElapsedTime(finalize_ms, ev[1], ev[2]), "event time");
 }
 
-void Plan::launch(cudaStream_t s) {
-  Engine& E = *eng;
+void Plan::run_device(cudaStream_t s) {
   for (cudaEvent_t& e : ev)
     if (!e) check_cuda(cudaEventCreate(&e), "cudaEventCreate");
-  prm.reqs = reqs.as<ReqDesc>();
-  prm.nreq = nreq;
-  prm.total_segs = total_segs;
-  prm.P = E.dP.as<uint32_t>();
-  prm.M = E.dM.as<uint64_t>();
-  prm.R = E.dR.as<uint32_t>();
-  prm.rstride = E.rstride;
-  prm.tileA = E.tileA.as<uint32_t>();
-  prm.tileB = E.tileB.as<uint32_t>();
-  prm.seg_bytes = cfg.seg_bytes;
-  prm.tier_split = tier_split_idx;
-  prm.tier_huge = tier_huge_idx;
-  prm.segs = segs.as<SegRec>();
-  prm.acc = acc.as<ReqAccum>();
-  prm.large = large.as<LargeGapRec>();
-  prm.n_large = nlarge.as<unsigned int>();
-  prm.large_cap = large_cap;
-  prm.flags = flags;
-  prm.bitmap = bitmap.as<uint32_t>();
-  if (nreq == 0) return;
-  check_cuda(cudaMemsetAsync(acc.ptr, 0, sizeof(ReqAccum) * nreq, s), "memset accumulators");
+  const uint32_t nacc = cap_req ? cap_req : nreq;
+  if (nacc == 0) return;
+  check_cuda(cudaMemsetAsync(acc.ptr, 0, sizeof(ReqAccum) * nacc, s), "memset accumulators");
   check_cuda(cudaMemsetAsync(nlarge.ptr, 0, sizeof(unsigned int), s), "memset large count");
+  check_cuda(cudaMemsetAsync(queue.ptr, 0, sizeof(unsigned long long), s), "memset work queue");
   check_cuda(cudaEventRecord(ev[0], s), "event");
-  check_cuda(launch_sieve(prm, grid, cfg.threads, s), "sieve_segments_kernel");
+  check_cuda(launch_sieve(prm, grid, threads, s), "sieve_segments_kernel");
   check_cuda(cudaEventRecord(ev[1], s), "event");
-  check_cuda(launch_finalize(reqs.as<ReqDesc>(), segs.as<SegRec>(), acc.as<ReqAccum>(),
-                             large.as<LargeGapRec>(), nlarge.as<unsigned int>(), large_cap,
-                             results.as<ReqResult>(), nreq, s),
+  check_cuda(launch_finalize(reqs.as<ReqDesc>(), hdr.as<BatchHdr>(), segs.as<SegRec>(),
+                             acc.as<ReqAccum>(), large.as<LargeGapRec>(),
+                             nlarge.as<unsigned int>(), large_cap, results.as<ReqResult>(), nacc, s),
              "finalize_kernel");
   check_cuda(cudaEventRecord(ev[2], s), "event");
 }
 
-const ReqResult* Plan::fetch(cudaStream_t s) {
-  host_results.reserve(sizeof(ReqResult) * std::max<uint32_t>(nreq, 1));
+void Plan::fetch_async(cudaStream_t s) {
   if (nreq)
     check_cuda(cudaMemcpyAsync(host_results.ptr, results.ptr, sizeof(ReqResult) * nreq,
                                cudaMemcpyDeviceToHost, s), "download results");
+}
+
+const ReqResult* Plan::finish() {
+  out.resize(nreq);
+  const ReqResult* r = static_cast<const ReqResult*>(host_results.ptr);
+  for (uint32_t i = 0; i < nreq; ++i) out[order[i]] = r[i];
+  return out.data();
+}
+
+const ReqResult* Plan::fetch(cudaStream_t s) {
+  fetch_async(s);
   check_cuda(cudaStreamSynchronize(s), "sieve run");
-  return static_cast<const ReqResult*>(host_results.ptr);
+  return finish();
 }
 
 std::vector<LargeGapRec> Plan::fetch_large(cudaStream_t s) {
@@ -329,6 +444,8 @@ std::vector<LargeGapRec> Plan::fetch_large(cudaStream_t s) {
                                cudaMemcpyDeviceToHost, s), "large gaps");
     check_cuda(cudaStreamSynchronize(s), "large gaps");
   }
+  // device request index -> caller's index
+  for (LargeGapRec& x : v) x.req = order[x.req];
   return v;
 }
 
@@ -361,8 +478,9 @@ uint64_t Plan::algorithmic_clears() const {
 }
 
 const ReqResult* Engine::run(uint32_t n, const uint64_t* a, const uint64_t* b,
-                             std::vector<LargeGapRec>* lg) {
-  scratch.prepare(n, a, b, 0);
+                             std::vector<LargeGapRec>* lg, bool gaps) {
+  std::vector<uint32_t> rf(n, gaps ? kReqGaps : 0u);
+  scratch.load(n, a, b, 0, rf.data());
   scratch.launch(stream);
   const ReqResult* r = scratch.fetch(stream);
   if (lg) *lg = scratch.fetch_large(stream);

@@ -61,21 +61,34 @@ struct Config {
 class Engine;
 
 // A prepared batch of ranges with its device buffers.
+//
+// load() writes the request descriptors and the batch header into pinned
+// staging memory; upload() copies them to the device; run_device() is the
+// device part (memsets, sieve, finalize) with fixed pointers and sizes, so it
+// can be captured into a CUDA graph once and replayed for every batch that
+// fits the plan's capacity (the kernels read the batch size from the device
+// header).  Requests are reordered by estimated cost, heaviest first, so the
+// work queue ends on light items; results come back in the caller's order.
 struct Plan {
   Engine* eng = nullptr;
+  int device = 0;
   uint32_t nreq = 0;
   uint64_t total_segs = 0;
+  uint32_t cap_req = 0;         // fixed capacity (graph-replayed plans); 0 = exact
+  uint64_t cap_segs = 0;
+  uint32_t seg_max = 0;         // shared-memory segment of the launch
+  uint32_t threads = 1024;
   uint32_t grid = 0;
-  Config cfg;
-  uint32_t tier_split_idx = 0;
-  uint32_t tier_huge_idx = 0;
-  std::vector<ReqDesc> host_reqs;
-  DevBuf reqs, segs, acc, large, nlarge, results, bitmap;
-  HostPinned host_results;
+  bool batch_mode = false;      // tune for throughput of many ranges
+  std::vector<ReqDesc> host_reqs;   // device order
+  std::vector<uint32_t> order;      // host_reqs[i] is the caller's request order[i]
+  DevBuf reqs, hdr, queue, segs, acc, large, nlarge, results, bitmap;
+  HostPinned stage;             // BatchHdr followed by ReqDesc[cap]
+  HostPinned host_results;      // ReqResult[] in device order
+  std::vector<ReqResult> out;   // caller order
   uint32_t large_cap = 1u << 16;
   uint32_t flags = 0;
   SieveParams prm{};
-  int device = 0;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // before sieve, after sieve, after finalize
 
   ~Plan();
@@ -86,16 +99,44 @@ struct Plan {
   // Kernels per run (sieve + finalize).
   static constexpr uint32_t kKernels = 2;
 
+  // Fix the capacity (requests, segments) of a graph-replayed plan.
+  void reserve_capacity(uint32_t max_req, uint64_t max_segs);
+  // rflags: per request kReqGaps (NULL = all requests want gaps)
+  void load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t flags,
+            const uint32_t* rflags = nullptr);
+  void upload(cudaStream_t s);
+  void run_device(cudaStream_t s);
   void prepare(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t flags);
-  void launch(cudaStream_t s);
-  // Copy results of the last run to host memory owned by the plan.
+  void launch(cudaStream_t s) { upload(s); run_device(s); }
+  // Capture run_device() into a CUDA graph (the plan must have a fixed
+  // capacity); launch_graph() replays it for the currently loaded batch.
+  void capture(cudaStream_t s);
+  void launch_graph(cudaStream_t s);
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  // Copy results of the last run to host memory (caller order).
   const ReqResult* fetch(cudaStream_t s);
+  // Queue the device-to-host copy of the results without waiting; finish()
+  // then reorders them (after the stream has reached that point).
+  void fetch_async(cudaStream_t s);
+  const ReqResult* finish();
   std::vector<LargeGapRec> fetch_large(cudaStream_t s);
   uint64_t algorithmic_clears() const;
   uint64_t wheel_bytes() const;
   // Durations of the sieve and finalize kernels of the last launch (CUDA
   // events recorded on the launching stream).
   void kernel_ms(float* sieve_ms, float* finalize_ms);
+  // Segments a range needs under this plan's tuning (for admission).
+  uint64_t segments_for(uint64_t a, uint64_t b) const;
+};
+
+// One entry of the offset-regime tuning table: ranges with b <= b_max and
+// width <= width_max use this segment size and tier split.
+struct TuneEntry {
+  uint64_t b_max;
+  uint64_t width_max;
+  uint32_t seg_bytes;
+  uint32_t tier_split;
 };
 
 class Engine {
@@ -123,11 +164,15 @@ class Engine {
   void ensure_table(uint64_t pmax);
   uint32_t primes_below_sq(uint64_t b) const;   // table primes p with p*p < b
   uint32_t index_of(uint32_t p) const;           // first table index with P >= p
-  Config tuned_for(uint64_t a, uint64_t b) const;
+  // Segment size and tier split for one range (offset-regime table, then the
+  // built-in rule); batch = tune for the throughput of a batch rather than
+  // the latency of this range alone.
+  Config tuned_for(uint64_t a, uint64_t b, bool batch = false) const;
+  std::vector<TuneEntry> tuning;
 
   // Run ranges synchronously on the engine stream.
   const ReqResult* run(uint32_t n, const uint64_t* a, const uint64_t* b,
-                       std::vector<LargeGapRec>* large = nullptr);
+                       std::vector<LargeGapRec>* large = nullptr, bool gaps = true);
 
  private:
   Engine() = default;
@@ -143,8 +188,9 @@ void to_public(const ReqResult& r, uint64_t a, uint64_t b, voss_range_stats_t* o
 size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads);
 cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads,
                          cudaStream_t stream);
-cudaError_t launch_finalize(const ReqDesc* reqs, const SegRec* segs, ReqAccum* acc,
-                            LargeGapRec* large, unsigned int* n_large, uint32_t large_cap,
-                            ReqResult* out, uint32_t nreq, cudaStream_t stream);
+cudaError_t launch_finalize(const ReqDesc* reqs, const BatchHdr* hdr, const SegRec* segs,
+                            ReqAccum* acc, LargeGapRec* large, unsigned int* n_large,
+                            uint32_t large_cap, ReqResult* out, uint32_t grid,
+                            cudaStream_t stream);
 
 }  // namespace vg

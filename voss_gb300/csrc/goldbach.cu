@@ -261,7 +261,7 @@ __global__ void extract_write_kernel(const uint32_t* __restrict__ wb, uint64_t n
 const uint32_t* sieve_bitmap(Engine& E, Plan& plan, uint64_t a, uint64_t b_excl, uint64_t* nwords) {
   plan.eng = &E;
   plan.device = E.device;
-  plan.prepare(1, &a, &b_excl, kFlagBitmap);
+  plan.load(1, &a, &b_excl, kFlagBitmap);
   plan.launch(E.stream);
   *nwords = (plan.host_reqs[0].k_hi - plan.host_reqs[0].k_lo + 3) / 4;
   return plan.bitmap.as<uint32_t>();
@@ -314,7 +314,7 @@ void goldbach_plan_launch(GoldbachPlan* g, cudaStream_t s) {
   // wheel bitmap of [0, N] (sieve kernel on the same stream)
   {
     uint64_t a = 0, b = g->N + 1;
-    if (!g->sieve.nreq || g->sieve.host_reqs[0].b != b) g->sieve.prepare(1, &a, &b, kFlagBitmap);
+    if (!g->sieve.nreq || g->sieve.host_reqs[0].b != b) g->sieve.load(1, &a, &b, kFlagBitmap);
     g->sieve.launch(s);
   }
   const uint32_t* wb = g->sieve.bitmap.as<uint32_t>();
@@ -435,7 +435,7 @@ std::vector<uint64_t> primes_in_range(Engine& E, uint64_t a, uint64_t b, uint64_
   if (b < 7) return seeds;
   // count first, so an oversized request fails before any bitmap is built
   uint64_t aa = a, bb = b + 1;
-  const uint64_t total = E.run(1, &aa, &bb)[0].count;
+  const uint64_t total = E.run(1, &aa, &bb, nullptr, false)[0].count;
   if (total > max_count) return std::vector<uint64_t>(max_count + 1, 0);
   Plan plan;
   uint64_t nw = 0;

@@ -1,0 +1,281 @@
+// serve.cpp -- continuous-batching request server on the GB300 sieve.
+//
+// The reference serves one query per Context: it allocates, sieves the whole
+// range host-serially segment by segment and frees, one call at a time
+// (library/src/primes/context.cu:212-559, 608-635).  Here requests arrive at
+// any time and are batched continuously:
+//   * K slots, each a stream with a fixed-capacity launch plan whose device
+//     part (memsets, the persistent sieve over a work queue, finalize) is a
+//     CUDA graph captured once and replayed for every batch;
+//   * a scheduler thread retires finished slots (event polling, results
+//     copied back asynchronously) and admits pending requests into free
+//     slots, FIFO, bounded by requests and segments per batch and by a
+//     device-memory budget over all batches in flight;
+//   * batches in different slots overlap on the device: CTAs of the next
+//     batch start as SMs free up from the previous one;
+//   * the sieving-prime table and tiles stay resident; count and Chebyshev
+//     requests skip the ordered gap scan.
+// A result is the same whether the request ran alone or in a batch.
+#include "serve.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+
+#include "voss/voss.h"
+
+namespace vg {
+
+static double now_us() {
+  using namespace std::chrono;
+  return duration<double, std::micro>(steady_clock::now().time_since_epoch()).count();
+}
+
+uint64_t Server::request_bytes(uint64_t segs) {
+  return segs * sizeof(SegRec) + sizeof(ReqAccum) + sizeof(ReqResult) + sizeof(ReqDesc);
+}
+
+Server::Server(Engine& e, const ServerConfig& c) : E(e), cfg(c) {
+  if (cfg.slots == 0 || cfg.slots > 64) throw Error(VOSS_ERR_INVALID_ARG, "slots must be in [1, 64]");
+  if (cfg.max_batch == 0) throw Error(VOSS_ERR_INVALID_ARG, "max_batch must be > 0");
+  if (cfg.max_segs == 0) throw Error(VOSS_ERR_INVALID_ARG, "max_segs must be > 0");
+  {
+    std::lock_guard<std::mutex> g(E.mu);
+    E.ensure_table(isqrt_u64(kMaxB - 1));     // graphs keep the table's pointers
+  }
+  slots.resize(cfg.slots);
+  for (auto& sp : slots) {
+    sp.reset(new Slot());
+    Slot& s = *sp;
+    s.plan.eng = &E;
+    s.plan.device = E.device;
+    s.plan.batch_mode = true;
+    s.plan.reserve_capacity(cfg.max_batch, cfg.max_segs);
+    check_cuda(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "server stream");
+    check_cuda(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "server event");
+  }
+  worker = std::thread([this] { loop(); });
+}
+
+Server::~Server() {
+  {
+    std::lock_guard<std::mutex> g(mu);
+    stop = true;
+  }
+  cv_work.notify_all();
+  if (worker.joinable()) worker.join();
+  for (auto& sp : slots) {
+    if (sp->stream) {
+      cudaStreamSynchronize(sp->stream);
+      cudaStreamDestroy(sp->stream);
+    }
+    if (sp->done) cudaEventDestroy(sp->done);
+  }
+}
+
+uint64_t Server::submit(uint64_t a, uint64_t b, uint32_t op) {
+  if (b > kMaxB) throw Error(VOSS_ERR_OUT_OF_RANGE, "range end exceeds 10^14 + 10^10 + 1");
+  if (op > kOpChebyshev) throw Error(VOSS_ERR_INVALID_ARG, "unknown request op");
+  const uint64_t segs = slots[0]->plan.segments_for(a, b);
+  if (segs > cfg.max_segs)
+    throw Error(VOSS_ERR_OUT_OF_RANGE, "range needs more segments than a server batch holds");
+  Ticket t;
+  t.a = a;
+  t.b = b;
+  t.op = op;
+  t.segs = segs;
+  t.bytes = request_bytes(segs);
+  t.t_submit = now_us();
+  uint64_t id;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    if (stop) throw Error(VOSS_ERR_INVALID_ARG, "server is shutting down");
+    id = next_id++;
+    tickets.emplace(id, t);
+    pending.push_back(id);
+    ++submitted;
+    if (!first_submit) first_submit = t.t_submit;
+  }
+  cv_work.notify_one();
+  return id;
+}
+
+bool Server::result(uint64_t id, bool wait, voss_range_stats_t* out, double* latency_us) {
+  std::unique_lock<std::mutex> g(mu);
+  auto it = tickets.find(id);
+  if (it == tickets.end()) throw Error(VOSS_ERR_INVALID_ARG, "unknown or already collected ticket");
+  if (!it->second.done) {
+    if (!wait) return false;
+    cv_done.wait(g, [&] { return tickets.at(id).done; });
+    it = tickets.find(id);
+  }
+  const Ticket& t = it->second;
+  if (t.error) {
+    const std::string msg = t.message;
+    tickets.erase(it);
+    throw Error(VOSS_ERR_CUDA, msg);
+  }
+  if (out) *out = t.res;
+  if (latency_us) *latency_us = t.t_done - t.t_submit;
+  tickets.erase(it);
+  return true;
+}
+
+void Server::drain() {
+  std::unique_lock<std::mutex> g(mu);
+  cv_done.wait(g, [&] { return pending.empty() && inflight == 0; });
+}
+
+void Server::metrics(voss_gb300_server_metrics_t* m) {
+  std::lock_guard<std::mutex> g(mu);
+  std::memset(m, 0, sizeof(*m));
+  m->submitted = submitted;
+  m->completed = completed;
+  m->batches = batches;
+  m->max_inflight_batches = max_inflight;
+  m->peak_admitted_bytes = peak_bytes;
+  m->pending = pending.size();
+  if (!lat.empty()) {
+    std::vector<double> v(lat);
+    std::sort(v.begin(), v.end());
+    auto q = [&](double f) { return v[std::min<size_t>(v.size() - 1, (size_t)(f * (v.size() - 1) + 0.5))]; };
+    m->p50_us = q(0.50);
+    m->p99_us = q(0.99);
+    double s = 0;
+    for (double x : v) s += x;
+    m->mean_us = s / v.size();
+  }
+  if (completed && last_done > first_submit)
+    m->req_per_s = completed / ((last_done - first_submit) * 1e-6);
+  m->mean_batch = batches ? (double)batched_requests / batches : 0.0;
+}
+
+void Server::reset_metrics() {
+  std::lock_guard<std::mutex> g(mu);
+  lat.clear();
+  completed = batches = batched_requests = 0;
+  submitted = pending.size() + inflight_requests;
+  first_submit = last_done = 0;
+  max_inflight = 0;
+  peak_bytes = 0;
+}
+
+void Server::retire(Slot& s) {
+  const cudaError_t q = cudaEventQuery(s.done);
+  if (q == cudaErrorNotReady) return;
+  std::string err;
+  const ReqResult* r = nullptr;
+  if (q != cudaSuccess) {
+    err = std::string("batch failed: ") + cudaGetErrorString(q);
+  } else {
+    r = s.plan.finish();
+  }
+  const double t = now_us();
+  std::lock_guard<std::mutex> g(mu);
+  for (size_t i = 0; i < s.ids.size(); ++i) {
+    Ticket& tk = tickets.at(s.ids[i]);
+    if (r) to_public(r[i], tk.a, tk.b, &tk.res);
+    else { tk.error = true; tk.message = err; }
+    tk.done = true;
+    tk.t_done = t;
+    lat.push_back(t - tk.t_submit);
+  }
+  completed += s.ids.size();
+  inflight_requests -= s.ids.size();
+  last_done = t;
+  inflight_bytes -= s.bytes;
+  --inflight;
+  s.busy = false;
+  s.ids.clear();
+  cv_done.notify_all();
+}
+
+bool Server::admit(Slot& s) {
+  std::vector<uint64_t> a, b;
+  std::vector<uint32_t> rf;
+  uint64_t segs = 0, bytes = 0;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    while (!pending.empty() && s.ids.size() < cfg.max_batch) {
+      const uint64_t id = pending.front();
+      const Ticket& t = tickets.at(id);
+      const bool first = s.ids.empty();
+      if (!first && segs + t.segs > cfg.max_segs) break;
+      // memory admission: what the request's segment records, accumulators
+      // and results occupy, against the budget over every batch in flight
+      if (inflight_bytes + bytes + t.bytes > cfg.mem_budget && !(first && inflight == 0)) break;
+      pending.pop_front();
+      s.ids.push_back(id);
+      a.push_back(t.a);
+      b.push_back(t.b);
+      rf.push_back(t.op == kOpTwins || t.op == kOpGapHist ? kReqGaps : 0u);
+      segs += t.segs;
+      bytes += t.bytes;
+    }
+    if (s.ids.empty()) return false;
+    inflight_bytes += bytes;
+    peak_bytes = std::max(peak_bytes, inflight_bytes);
+    ++inflight;
+    inflight_requests += s.ids.size();
+    max_inflight = std::max<uint64_t>(max_inflight, inflight);
+    ++batches;
+    batched_requests += s.ids.size();
+  }
+  s.bytes = bytes;
+  try {
+    s.plan.load((uint32_t)a.size(), a.data(), b.data(), 0, rf.data());
+    s.plan.upload(s.stream);
+    if (cfg.use_graphs) s.plan.launch_graph(s.stream);
+    else s.plan.run_device(s.stream);
+    s.plan.fetch_async(s.stream);
+    check_cuda(cudaEventRecord(s.done, s.stream), "server event");
+  } catch (const std::exception& e) {
+    std::lock_guard<std::mutex> g(mu);
+    const double t = now_us();
+    for (uint64_t id : s.ids) {
+      Ticket& tk = tickets.at(id);
+      tk.error = true;
+      tk.message = e.what();
+      tk.done = true;
+      tk.t_done = t;
+    }
+    inflight_requests -= s.ids.size();
+    inflight_bytes -= bytes;
+    --inflight;
+    s.ids.clear();
+    cv_done.notify_all();
+    return false;
+  }
+  s.busy = true;
+  return true;
+}
+
+void Server::loop() {
+  int dev = E.device;
+  cudaSetDevice(dev);
+  for (;;) {
+    bool progressed = false;
+    for (auto& sp : slots)
+      if (sp->busy) {
+        const bool was = sp->busy;
+        retire(*sp);
+        progressed |= was && !sp->busy;
+      }
+    for (auto& sp : slots)
+      if (!sp->busy) {
+        if (!admit(*sp)) break;
+        progressed = true;
+      }
+    if (progressed) continue;
+    std::unique_lock<std::mutex> g(mu);
+    if (stop && pending.empty() && inflight == 0) break;
+    if (inflight == 0) {
+      cv_work.wait_for(g, std::chrono::milliseconds(5));     // idle: wait for submissions
+    } else {
+      g.unlock();
+      std::this_thread::sleep_for(std::chrono::microseconds(20));   // batches in flight: poll
+    }
+  }
+}
+
+}  // namespace vg

@@ -109,8 +109,8 @@ sieve_segments_kernel(const SieveParams prm) {
   uint32_t* shist = seg + (prm.seg_bytes >> 2);
   WarpRec* wrec = reinterpret_cast<WarpRec*>(shist + kSmemHistCopies * kSmemStride);
 
-  __shared__ uint64_t s_k0, s_seg_in_req;
-  __shared__ uint32_t s_req, s_nbytes, s_np, s_ctr;
+  __shared__ uint64_t s_k0, s_seg_in_req, s_item;
+  __shared__ uint32_t s_req, s_nbytes, s_np, s_ctr, s_split, s_huge, s_rflags;
   __shared__ uint32_t s_vtab[32];      // bit b of a word -> 30*(b/8) + W30[b%8]
 
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -121,18 +121,28 @@ sieve_segments_kernel(const SieveParams prm) {
   if (tid == 0) s_ctr = 0;
   int cur_req = -1;
 
-  for (uint64_t item = blockIdx.x; item < prm.total_segs; item += gridDim.x) {
+  const uint64_t total_segs = prm.hdr->total_segs;
+  const uint32_t nreq = prm.hdr->nreq;
+  for (;;) {
+    // work queue: the next (request, segment) item, heaviest requests first
+    if (tid == 0) s_item = atomicAdd(prm.queue, 1ull);
+    __syncthreads();
+    const uint64_t item = s_item;
+    if (item >= total_segs) break;
     if (tid == 0) {
-      uint32_t lo = 0, hi = prm.nreq;             // last request with seg_base <= item
+      uint32_t lo = 0, hi = nreq;                 // last request with seg_base <= item
       while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         if (prm.reqs[mid].seg_base <= item) lo = mid; else hi = mid;
       }
       const ReqDesc& R = prm.reqs[lo];
       const uint64_t si = item - R.seg_base;
-      const uint64_t k0 = R.k_lo + si * prm.seg_bytes;
+      const uint64_t k0 = R.k_lo + si * R.seg_bytes;
       const uint64_t left = R.k_hi - k0;
-      const uint32_t nb = left < prm.seg_bytes ? (uint32_t)left : prm.seg_bytes;
+      const uint32_t nb = left < R.seg_bytes ? (uint32_t)left : R.seg_bytes;
+      s_split = R.tier_split;
+      s_huge = R.tier_huge;
+      s_rflags = R.rflags;
       // table primes with p*p below the segment's upper end
       const uint64_t hi_num = 30ull * (k0 + nb);
       uint32_t a = 0, b = R.nprimes;
@@ -181,8 +191,8 @@ sieve_segments_kernel(const SieveParams prm) {
     {
       // unit layout: [0, nsmall) small primes, then 32-prime units of the mid
       // tier (split <= p < S), then 32-prime units of the huge tier (p >= S)
-      const uint32_t nsmall = prm.tier_split < np ? prm.tier_split : np;
-      const uint32_t hbeg = prm.tier_huge < np ? max(prm.tier_huge, nsmall) : np;
+      const uint32_t nsmall = s_split < np ? s_split : np;
+      const uint32_t hbeg = s_huge < np ? max(s_huge, nsmall) : np;
       const uint32_t nmidu = (hbeg - nsmall + 31u) / 32u;
       const uint32_t nunits = nsmall + nmidu + (np - hbeg + 31u) / 32u;
       const uint32_t o = lane & 7u, h = lane >> 3;
@@ -296,6 +306,7 @@ sieve_segments_kernel(const SieveParams prm) {
       const uint32_t wbeg = min(tid * run, nwords);
       const uint32_t wend = min(wbeg + run, nwords);
       uint32_t first1 = 0, last1 = 0, cnt = 0, c41 = 0, c31 = 0, maxg = 0, maxgs = 0;
+      const bool gaps = (s_rflags & kReqGaps) != 0;
       for (uint32_t wi = wbeg; wi < wend; ++wi) {
         uint32_t w = seg[wi];
         if (!w) continue;
@@ -303,6 +314,11 @@ sieve_segments_kernel(const SieveParams prm) {
         c41 += __popc(w & m41);
         c31 += __popc(w & 0x2B2B2B2Bu);
         const uint32_t vb = 120u * wi;
+        if (!gaps) {                        // counts only: keep first and last
+          if (!first1) first1 = vb + s_vtab[__ffs(w) - 1] + 1u;
+          last1 = vb + s_vtab[31 - __clz(w)] + 1u;
+          continue;
+        }
         do {
           const uint32_t bp = (uint32_t)__ffs(w) - 1u;
           w &= w - 1u;
@@ -321,7 +337,7 @@ sieve_segments_kernel(const SieveParams prm) {
       }
       uint32_t prev1 = __shfl_up_sync(0xFFFFFFFFu, sc, 1);
       if (lane == 0) prev1 = 0;
-      if (first1 && prev1) record_gap(sk, prev1 - 1u, first1 - 1u, maxg, maxgs);
+      if (gaps && first1 && prev1) record_gap(sk, prev1 - 1u, first1 - 1u, maxg, maxgs);
       const uint32_t wlast = __shfl_sync(0xFFFFFFFFu, sc, 31);
       const uint32_t wfirst = __reduce_min_sync(0xFFFFFFFFu, first1 ? first1 : 0xFFFFFFFFu);
       cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
@@ -342,7 +358,7 @@ sieve_segments_kernel(const SieveParams prm) {
         for (uint32_t wv = 0; wv < nwarps; ++wv) {
           const WarpRec r = wrec[wv];
           if (r.first1) {
-            if (run1) record_gap(sk, run1 - 1u, r.first1 - 1u, bg, bs);
+            if (run1 && gaps) record_gap(sk, run1 - 1u, r.first1 - 1u, bg, bs);
             else fst1 = r.first1;
             run1 = r.last1;
           }
@@ -379,10 +395,11 @@ sieve_segments_kernel(const SieveParams prm) {
 // largest gap, and the final counts (the reference's host-side conventions,
 // context.cu:321-322,462-524, restated for a half-open [a, b)).
 __global__ void __launch_bounds__(256)
-finalize_kernel(const ReqDesc* __restrict__ reqs, const SegRec* __restrict__ segs,
-                ReqAccum* __restrict__ acc, LargeGapRec* large, unsigned int* n_large,
-                uint32_t large_cap, ReqResult* __restrict__ out) {
+finalize_kernel(const ReqDesc* __restrict__ reqs, const BatchHdr* __restrict__ hdr,
+                const SegRec* __restrict__ segs, ReqAccum* __restrict__ acc, LargeGapRec* large,
+                unsigned int* n_large, uint32_t large_cap, ReqResult* __restrict__ out) {
   const uint32_t r = blockIdx.x, tid = threadIdx.x;
+  if (r >= hdr->nreq) return;       // fixed-size launches (graph replay) cover capacity
   const ReqDesc R = reqs[r];
   ReqAccum* A = acc + r;
   const SegRec* S = segs + R.seg_base;
@@ -396,11 +413,12 @@ finalize_kernel(const ReqDesc* __restrict__ reqs, const SegRec* __restrict__ seg
   auto consider = [&](uint64_t g, uint64_t st) {
     if (g > bg || (g == bg && g && st < bs)) { bg = g; bs = st; }
   };
-  if (tid == 0) {
+  if (tid == 0 && (R.rflags & kReqGaps)) {
     if (in2 && in3) { atomicAdd(&A->hist[0], 1ull); consider(1, 2); }
     if (in3 && in5) { atomicAdd(&A->hist[1], 1ull); consider(2, 3); }
   }
-  for (uint64_t i = tid; i < R.nseg; i += blockDim.x) {
+  const bool want_gaps = (R.rflags & kReqGaps) != 0;
+  for (uint64_t i = want_gaps ? tid : R.nseg; i < R.nseg; i += blockDim.x) {
     const SegRec s = S[i];
     if (s.max_gap) consider(s.max_gap, s.max_gap_start);
     if (!s.first) continue;
@@ -465,23 +483,24 @@ size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads) {
 cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads,
                          cudaStream_t stream) {
   const size_t smem = sieve_smem_bytes(prm.seg_bytes, threads);
-  static size_t smem_set = 0;   // the attribute is raised once, before any capture
+  static size_t smem_set = 0;   // raised once per size, outside stream capture
   if (smem > smem_set) {
     cudaError_t e = cudaFuncSetAttribute(sieve_segments_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     smem_set = smem;
   }
-  if (grid == 0 || prm.total_segs == 0) return cudaSuccess;
+  if (grid == 0) return cudaSuccess;
   sieve_segments_kernel<<<grid, threads, smem, stream>>>(prm);
   return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(const ReqDesc* reqs, const SegRec* segs, ReqAccum* acc,
-                            LargeGapRec* large, unsigned int* n_large, uint32_t large_cap,
-                            ReqResult* out, uint32_t nreq, cudaStream_t stream) {
-  if (nreq == 0) return cudaSuccess;
-  finalize_kernel<<<nreq, 256, 0, stream>>>(reqs, segs, acc, large, n_large, large_cap, out);
+cudaError_t launch_finalize(const ReqDesc* reqs, const BatchHdr* hdr, const SegRec* segs,
+                            ReqAccum* acc, LargeGapRec* large, unsigned int* n_large,
+                            uint32_t large_cap, ReqResult* out, uint32_t grid,
+                            cudaStream_t stream) {
+  if (grid == 0) return cudaSuccess;
+  finalize_kernel<<<grid, 256, 0, stream>>>(reqs, hdr, segs, acc, large, n_large, large_cap, out);
   return cudaGetLastError();
 }
 

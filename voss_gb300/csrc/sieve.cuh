@@ -25,13 +25,28 @@ constexpr int kMaxThreads = 1024;
 // Flags of one launch.
 constexpr uint32_t kFlagBitmap = 1u;     // also write the sieved words out
 
-// One range request, half-open [a, b), as the device sees it.
+// One range request, half-open [a, b), as the device sees it.  Each request
+// carries its own segment size and tier boundaries (chosen per offset regime).
 struct ReqDesc {
   uint64_t a, b;
   uint64_t k_lo, k_hi;      // wheel bytes [k_lo, k_hi) that cover [a, b)
   uint64_t seg_base;        // index of the request's first segment
   uint64_t nseg;
   uint32_t nprimes;         // table primes p (>= 37) with p*p < b
+  uint32_t seg_bytes;       // this request's segment size (<= the launch's)
+  uint32_t tier_split;      // table index of the first mid-tier prime
+  uint32_t tier_huge;       // table index of the first prime >= seg_bytes
+  uint32_t rflags;          // kReqGaps: gap histogram and largest gap wanted
+  uint32_t pad;
+};
+
+constexpr uint32_t kReqGaps = 1u;
+
+// Batch header in device memory: a captured launch reads its size from here,
+// so one CUDA graph serves every batch of a slot.
+struct BatchHdr {
+  uint64_t total_segs;
+  uint32_t nreq;
   uint32_t pad;
 };
 
@@ -70,17 +85,15 @@ struct ReqResult {
 
 struct SieveParams {
   const ReqDesc* reqs;
-  uint32_t nreq;
-  uint64_t total_segs;
+  const BatchHdr* hdr;
+  unsigned long long* queue;   // work-queue head: next (request, segment) item
   const uint32_t* P;         // table primes >= 37, ascending
   const uint64_t* M;         // floor((2^64-1)/p), for x mod p
   const uint32_t* R;         // R[o * rstride + i]: k = R (mod p) <=> p | 30k+W30[o]
   uint64_t rstride;
   const uint32_t* tileA;     // presieve tiles, extended past their period
   const uint32_t* tileB;
-  uint32_t seg_bytes;        // S, a multiple of 128
-  uint32_t tier_split;       // table index of the first mid-tier prime
-  uint32_t tier_huge;        // table index of the first prime >= seg_bytes
+  uint32_t seg_bytes;        // the largest segment of the launch (shared memory)
   SegRec* segs;
   ReqAccum* acc;
   LargeGapRec* large;
