@@ -91,6 +91,17 @@ def test_minimal_profile_counts(vg):
         assert ctx.prime_count() == 5761455
 
 
+def test_count_only_batch_keeps_first_and_last(vg, oracle_lib):
+    """Count-only requests (no gap scan) still report first/last prime."""
+    from voss_gb300.serve import Server
+    with Server(slots=1) as srv:
+        for a, b in ((1181320, 1186543), (0, 10**8), (10**12 + 7, 10**12 + 3 * 10**7)):
+            got, _ = srv.result(srv.submit(a, b, 0))
+            orc = oracle_lib.range_stats(a, b)
+            assert (got.count, got.first_prime, got.last_prime) == (orc["count"], orc["first"], orc["last"])
+            assert (got.pi_4_1, got.pi_3_1) == (orc["pi_4_1"], orc["pi_3_1"])
+
+
 def test_random_windows_vs_oracle(vg, oracle_lib):
     rng = random.Random(7)
     cases = [(0, 1), (0, 2), (0, 7), (0, 8), (1, 60), (29, 31), (30, 31), (31, 32), (0, 30 * 196608 + 1),

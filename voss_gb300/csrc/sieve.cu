@@ -358,8 +358,8 @@ sieve_segments_kernel(const SieveParams prm) {
         for (uint32_t wv = 0; wv < nwarps; ++wv) {
           const WarpRec r = wrec[wv];
           if (r.first1) {
-            if (run1 && gaps) record_gap(sk, run1 - 1u, r.first1 - 1u, bg, bs);
-            else fst1 = r.first1;
+            if (!run1) fst1 = r.first1;
+            else if (gaps) record_gap(sk, run1 - 1u, r.first1 - 1u, bg, bs);
             run1 = r.last1;
           }
           if (r.maxg > bg || (r.maxg == bg && r.maxg && r.maxgs < bs)) { bg = r.maxg; bs = r.maxgs; }
