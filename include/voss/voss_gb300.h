@@ -56,6 +56,25 @@ int voss_primes_range_stats_ex(uint64_t a, uint64_t b, voss_range_stats_t* out,
 int voss_primes_range_stats_batch(uint64_t n, const uint64_t* a, const uint64_t* b,
                                   voss_range_stats_t* out);
 
+/* voss_primes_range_stats for callers that cannot allocate device memory
+ * while they run -- for instance a process whose device memory belongs to
+ * another framework's caching allocator, or a latency-critical loop where
+ * cudaMalloc / cudaFree would synchronize the device.  The reference has no
+ * counterpart.  The call allocates nothing: its scratch, sieving-prime table
+ * and presieve tiles live in static device arrays of this library (about
+ * 6.6 MB per GPU that loads it, held until the process exits).  The caller
+ * passes the range and `out`, device-accessible memory that receives the
+ * result in stream order on `stream` (a cudaStream_t, NULL = legacy default
+ * stream); the call returns once the work is enqueued.
+ * Limits: b <= 2^40 and a width of at most 65536 segments of 221184 bytes
+ * (about 4.3 * 10^11 integers); beyond them VOSS_ERR_OUT_OF_RANGE.
+ * The first call on a device sets that device up; make it before any stream
+ * capture.  All calls share one scratch array and leave their contents
+ * behind: calls in sequence are independent, calls that overlap on the GPU
+ * race and give wrong results. */
+int voss_primes_range_stats_noalloc(uint64_t a, uint64_t b, voss_range_stats_t* out,
+                                    void* stream);
+
 /* Tunables of the segmented sieve.  seg_bytes: shared-memory segment in
  * bytes (30 integers each), a multiple of 128, at most 221184.  threads: CTA
  * size (multiple of 32, <= 1024).  tier_split: primes below it are marked a

@@ -102,6 +102,7 @@ _SIGS = {
     "voss_primes_range_stats": ([u64, u64, P(VossRangeStats)], c_int),
     "voss_primes_range_stats_ex": ([u64, u64, P(VossRangeStats), P(u64)], c_int),
     "voss_primes_range_stats_batch": ([u64, P(u64), P(u64), P(VossRangeStats)], c_int),
+    "voss_primes_range_stats_noalloc": ([u64, u64, vp, vp], c_int),
     "voss_gb300_get_config": ([P(VossConfig)], c_int),
     "voss_gb300_set_config": ([P(VossConfig)], c_int),
     "voss_gb300_plan_create": ([u64, P(u64), P(u64), P(vp)], c_int),

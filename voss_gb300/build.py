@@ -21,7 +21,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libvoss.so"
-SOURCES = ["sieve.cu", "goldbach.cu", "probe.cu", "engine.cpp", "serve.cpp", "capi.cpp"]
+SOURCES = ["sieve.cu", "goldbach.cu", "probe.cu", "noalloc.cu", "engine.cpp", "serve.cpp", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
