@@ -92,6 +92,20 @@ typedef struct {
 int voss_gb300_get_config(voss_gb300_config_t* out);
 int voss_gb300_set_config(const voss_gb300_config_t* cfg);
 
+/* Offset-regime tuning table (written by voss_gb300/autotune.py, a built-in
+ * copy ships in the library): a range [a, b) uses the first entry with
+ * b <= b_max and b - a <= width_max.  n = 0 clears the table (the built-in
+ * rule then applies). */
+typedef struct {
+    uint64_t b_max;
+    uint64_t width_max;
+    uint32_t seg_bytes;
+    uint32_t tier_split;
+} voss_gb300_tune_entry_t;
+
+int voss_gb300_set_tuning(uint32_t n, const voss_gb300_tune_entry_t* entries);
+int voss_gb300_get_tuning(uint32_t cap, voss_gb300_tune_entry_t* entries, uint32_t* n);
+
 /* A launch plan: the requests, their segment list and all device buffers,
  * prepared once and launched any number of times on a caller's stream (also
  * inside stream capture, after the first launch).  Used to time the device

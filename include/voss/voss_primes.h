@@ -7,8 +7,8 @@
  * reference's, bit for bit, on the same inputs.
  *
  * Entry points outside the sieve (Miller-Rabin, factorisation, Mersenne /
- * Fermat tests, single-n Goldbach partitions, nth/next/prev) are exported so
- * that the binding loads, and return VOSS_ERR_INTERNAL with a message.
+ * Fermat tests, single-n Goldbach partitions) are exported so that the
+ * binding loads, and return VOSS_ERR_INTERNAL with a message.
  */
 #ifndef VOSS_PRIMES_H
 #define VOSS_PRIMES_H
@@ -80,10 +80,15 @@ int voss_primes_in_range(uint64_t a, uint64_t b,
 int voss_primes_in_range_with_limit(uint64_t a, uint64_t b, uint64_t max_count,
                                     uint64_t** out_array, uint64_t* out_count);
 
-/* Outside the sieve; exported for the binding (voss_primes.h:109-147). */
+/* n-th prime (1-based, n <= 5*10^7), smallest prime > x, largest prime < x,
+ * all on the GPU sieve (voss_primes.h:109-116; nth.cu:40-103,
+ * next_prev.cu:22-83 validate the same way).  x must stay below
+ * 10^14 + 10^10, the sieve's range; beyond it VOSS_ERR_OUT_OF_RANGE. */
 int voss_primes_nth(uint64_t n, uint64_t* out_prime);
 int voss_primes_next(uint64_t x, uint64_t* out_prime);
 int voss_primes_prev(uint64_t x, uint64_t* out_prime);
+
+/* Outside the sieve; exported for the binding (voss_primes.h:121-147). */
 int voss_primes_is_prime(uint64_t x, int* out);
 int voss_primes_factorize(uint64_t x, uint64_t** out_array, uint64_t* out_count);
 int voss_primes_is_mersenne_prime(uint32_t p, int* out);

@@ -60,6 +60,17 @@ def test_reference_symbol_set_present(lib):
         getattr(lib, n)
 
 
+def test_nth_next_prev_validation_without_gpu(lib):
+    out = ctypes.c_uint64(0)
+    assert lib.voss_primes_nth(ctypes.c_uint64(0), ctypes.byref(out)) == 1
+    assert lib.voss_primes_nth(ctypes.c_uint64(50000001), ctypes.byref(out)) == 2
+    assert lib.voss_primes_nth(ctypes.c_uint64(4), ctypes.byref(out)) == 0 and out.value == 7
+    assert lib.voss_primes_next(ctypes.c_uint64(1), ctypes.byref(out)) == 0 and out.value == 2
+    assert lib.voss_primes_prev(ctypes.c_uint64(2), ctypes.byref(out)) == 1
+    assert lib.voss_primes_prev(ctypes.c_uint64(3), ctypes.byref(out)) == 0 and out.value == 2
+    assert lib.voss_primes_next(ctypes.c_uint64(10), None) == 6
+
+
 def test_error_codes_and_validation(lib):
     lib.voss_strerror.restype = ctypes.c_char_p
     lib.voss_get_last_error.restype = ctypes.c_char_p
@@ -100,7 +111,7 @@ def test_error_codes_and_validation(lib):
 def test_outside_entry_points_fail_loudly(lib):
     out = ctypes.c_uint64(0)
     lib.voss_get_last_error.restype = ctypes.c_char_p
-    assert lib.voss_primes_nth(ctypes.c_uint64(5), ctypes.byref(out)) == 7
+    assert lib.voss_primes_is_prime(ctypes.c_uint64(5), ctypes.byref(ctypes.c_int())) == 7
     assert b"outside the sieve" in lib.voss_get_last_error()
 
 

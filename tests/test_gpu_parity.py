@@ -268,3 +268,27 @@ def test_configs_agree(vg, oracle_lib):
                 assert_range_equal(vg.range_stats(a, b, full=True), w, (cfg, a, b))
     finally:
         vg.primes.set_config(**base)
+
+
+def test_nth_next_prev(vg, oracle_lib):
+    # test_primes.py:245-303
+    assert [vg.primes.nth(k) for k in (1, 2, 3, 10, 100, 1000)] == [2, 3, 5, 29, 541, 7919]
+    assert vg.primes.next_prime(1) == 2 and vg.primes.next_prime(2) == 3
+    assert vg.primes.next_prime(10) == 11 and vg.primes.next_prime(100) == 101
+    assert vg.primes.next_prime(10**6) == 1000003 and vg.primes.next_prime(10**9) == 1000000007
+    assert vg.primes.prev_prime(3) == 2 and vg.primes.prev_prime(5) == 3
+    assert vg.primes.prev_prime(10) == 7 and vg.primes.prev_prime(1000) == 997
+    assert vg.primes.prev_prime(10**9) == 999999937
+    with pytest.raises(vg.VossError):
+        vg.primes.prev_prime(2)
+    with pytest.raises(vg.VossError):
+        vg.primes.nth(0)
+    with pytest.raises(vg.VossError):
+        vg.primes.nth(50000001)
+    for x in (100, 1000, 10**6, 10**12 + 39, 10**14 - 1000):     # test_primes.py:294-303
+        nxt, prv = vg.primes.next_prime(x), vg.primes.prev_prime(x)
+        assert vg.primes.in_range(x + 1, nxt)[0] == nxt
+        assert vg.primes.in_range(prv, x - 1)[-1] == prv
+    for k in (6, 7, 1234, 78498, 78499, 5761455, 50000000):
+        p = vg.primes.nth(k)
+        assert oracle_lib.range_stats(0, p + 1)["count"] == k and oracle_lib.range_stats(p, p + 1)["count"] == 1

@@ -98,6 +98,9 @@ _SIGS = {
     "voss_primes_in_range": ([u64, u64, P(P(u64)), P(u64)], c_int),
     "voss_primes_in_range_with_limit": ([u64, u64, u64, P(P(u64)), P(u64)], c_int),
     "voss_primes_goldbach_test_upto": ([u64, P(P(u64)), P(u64), u64], c_int),
+    "voss_primes_nth": ([u64, P(u64)], c_int),
+    "voss_primes_next": ([u64, P(u64)], c_int),
+    "voss_primes_prev": ([u64, P(u64)], c_int),
     # voss_gb300.h
     "voss_primes_range_stats": ([u64, u64, P(VossRangeStats)], c_int),
     "voss_primes_range_stats_ex": ([u64, u64, P(VossRangeStats), P(u64)], c_int),

@@ -490,9 +490,94 @@ extern "C" int voss_primes_goldbach_test_upto(uint64_t N, uint64_t** out_ce, uin
   set_err(std::string(name) + " is outside the sieve hot path and is not provided by this library"); \
   return VOSS_ERR_INTERNAL;
 
-extern "C" int voss_primes_nth(uint64_t, uint64_t*) { VOSS_OUTSIDE("voss_primes_nth") }
-extern "C" int voss_primes_next(uint64_t, uint64_t*) { VOSS_OUTSIDE("voss_primes_next") }
-extern "C" int voss_primes_prev(uint64_t, uint64_t*) { VOSS_OUTSIDE("voss_primes_prev") }
+// nth / next / prev on the GPU sieve (the reference walks candidates with
+// Miller-Rabin or a host vector<bool> sieve, nth.cu:40-103, next_prev.cu:22-83;
+// same validation, limits and codes).  The sieve covers numbers below
+// 10^14 + 10^10; beyond that these return VOSS_ERR_OUT_OF_RANGE.
+namespace {
+
+// smallest prime in [lo, hi), 0 if none (count-only run: first/last kept)
+uint64_t first_prime_in(vg::Engine& E, uint64_t lo, uint64_t hi) {
+  return E.run(1, &lo, &hi, nullptr, false)[0].first;
+}
+uint64_t last_prime_in(vg::Engine& E, uint64_t lo, uint64_t hi) {
+  return E.run(1, &lo, &hi, nullptr, false)[0].last;
+}
+constexpr uint64_t kSearchMax = 100000000ull;   // the reference's MAX_SEARCH
+
+}  // namespace
+
+extern "C" int voss_primes_next(uint64_t x, uint64_t* out) {
+  if (!out) { set_err("out pointer is null"); return VOSS_ERR_INVALID_ARG; }
+  if (x < 2) { *out = 2; return VOSS_OK; }
+  if (x >= vg::kMaxB - 1) { set_err("x exceeds the sieve's range (10^14 + 10^10)"); return VOSS_ERR_OUT_OF_RANGE; }
+  return guarded([&] {
+    vg::Engine& E = vg::Engine::for_current_device();
+    std::lock_guard<std::mutex> g(E.mu);
+    uint64_t w = 4096;
+    for (uint64_t lo = x + 1; lo - (x + 1) < kSearchMax && lo < vg::kMaxB; lo += w, w *= 2) {
+      const uint64_t hi = std::min<uint64_t>(lo + w, vg::kMaxB);
+      const uint64_t p = first_prime_in(E, lo, hi);
+      if (p) { *out = p; return VOSS_OK; }
+    }
+    set_err("no prime found within search limit");
+    return VOSS_ERR_OUT_OF_RANGE;
+  }, VOSS_ERR_CUDA);
+}
+
+extern "C" int voss_primes_prev(uint64_t x, uint64_t* out) {
+  if (!out) { set_err("out pointer is null"); return VOSS_ERR_INVALID_ARG; }
+  if (x <= 2) { set_err("no prime < " + std::to_string(x)); return VOSS_ERR_INVALID_N; }
+  if (x == 3) { *out = 2; return VOSS_OK; }
+  if (x > vg::kMaxB) { set_err("x exceeds the sieve's range (10^14 + 10^10)"); return VOSS_ERR_OUT_OF_RANGE; }
+  return guarded([&] {
+    vg::Engine& E = vg::Engine::for_current_device();
+    std::lock_guard<std::mutex> g(E.mu);
+    uint64_t w = 4096;
+    for (uint64_t hi = x; hi > 2 && x - hi < kSearchMax; w *= 2) {
+      const uint64_t lo = hi > w ? hi - w : 0;
+      const uint64_t p = last_prime_in(E, lo, hi);
+      if (p) { *out = p; return VOSS_OK; }
+      hi = lo;
+    }
+    *out = 2;
+    return VOSS_OK;
+  }, VOSS_ERR_CUDA);
+}
+
+extern "C" int voss_primes_nth(uint64_t n, uint64_t* out) {
+  if (!out) { set_err("out pointer is null"); return VOSS_ERR_INVALID_ARG; }
+  if (n == 0) { set_err("n must be >= 1 (1-indexed)"); return VOSS_ERR_INVALID_N; }
+  if (n > 50000000ull) { set_err("n exceeds maximum (50,000,000)"); return VOSS_ERR_OUT_OF_RANGE; }
+  static const uint64_t first[6] = {0, 2, 3, 5, 7, 11};
+  if (n <= 5) { *out = first[n]; return VOSS_OK; }
+  return guarded([&] {
+    vg::Engine& E = vg::Engine::for_current_device();
+    std::lock_guard<std::mutex> g(E.mu);
+    // estimate p_n ~ n (ln n + ln ln n - 1 + (ln ln n - 2) / ln n), count pi(est)
+    // on the GPU, then list the primes between the estimate and p_n
+    const double nf = (double)n, L = std::log(nf), LL = std::log(L);
+    const uint64_t est = (uint64_t)(nf * (L + LL - 1.0 + (LL - 2.0) / L));
+    uint64_t a = 0, b = est + 1;
+    const uint64_t c = E.run(1, &a, &b, nullptr, false)[0].count;     // pi(est)
+    const uint64_t span = (uint64_t)(L * 1.5 * (double)(c > n ? c - n : n - c) + 4096.0);
+    if (c >= n) {                       // p_n <= est: the (c - n + 1)-th largest prime <= est
+      const uint64_t lo = est > span ? est - span : 0;
+      for (uint64_t lo2 = lo;; lo2 = lo2 > span ? lo2 - span : 0) {
+        std::vector<uint64_t> v = vg::primes_in_range(E, lo2, est, ~0ull >> 1);
+        if (v.size() >= c - n + 1) { *out = v[v.size() - (c - n + 1)]; return VOSS_OK; }
+        if (lo2 == 0) break;
+      }
+    } else {                            // p_n > est: the (n - c)-th prime after est
+      for (uint64_t hi = est + span;; hi += span) {
+        std::vector<uint64_t> v = vg::primes_in_range(E, est + 1, hi, ~0ull >> 1);
+        if (v.size() >= n - c) { *out = v[n - c - 1]; return VOSS_OK; }
+      }
+    }
+    set_err("internal: could not locate the n-th prime");
+    return VOSS_ERR_INTERNAL;
+  }, VOSS_ERR_CUDA);
+}
 extern "C" int voss_primes_is_prime(uint64_t, int*) { VOSS_OUTSIDE("voss_primes_is_prime") }
 extern "C" int voss_primes_factorize(uint64_t, uint64_t**, uint64_t*) { VOSS_OUTSIDE("voss_primes_factorize") }
 extern "C" int voss_primes_is_mersenne_prime(uint32_t, int*) { VOSS_OUTSIDE("voss_primes_is_mersenne_prime") }
@@ -586,6 +671,37 @@ extern "C" int voss_gb300_set_config(const voss_gb300_config_t* c) {
     if (vg::sieve_smem_bytes(n.seg_bytes, n.threads) > E.max_smem_optin)
       throw vg::Error(VOSS_ERR_INVALID_ARG, "segment does not fit in shared memory");
     E.cfg = n;
+    return VOSS_OK;
+  }, VOSS_ERR_INTERNAL);
+}
+
+extern "C" int voss_gb300_set_tuning(uint32_t n, const voss_gb300_tune_entry_t* e) {
+  if (n && !e) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+  for (uint32_t i = 0; i < n; ++i)
+    if (e[i].seg_bytes < 1024 || e[i].seg_bytes > 221184 || e[i].seg_bytes % 128 ||
+        e[i].tier_split < vg::kFirstTablePrime) {
+      set_err("tuning entry out of range (seg_bytes in [1024, 221184], multiple of 128; tier_split >= 37)");
+      return VOSS_ERR_INVALID_ARG;
+    }
+  return guarded([&] {
+    vg::Engine& E = vg::Engine::for_current_device();
+    std::lock_guard<std::mutex> g(E.mu);
+    E.tuning.clear();
+    for (uint32_t i = 0; i < n; ++i)
+      E.tuning.push_back(vg::TuneEntry{e[i].b_max, e[i].width_max, e[i].seg_bytes, e[i].tier_split});
+    return VOSS_OK;
+  }, VOSS_ERR_INTERNAL);
+}
+
+extern "C" int voss_gb300_get_tuning(uint32_t cap, voss_gb300_tune_entry_t* e, uint32_t* n) {
+  if (!n || (cap && !e)) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+  return guarded([&] {
+    vg::Engine& E = vg::Engine::for_current_device();
+    std::lock_guard<std::mutex> g(E.mu);
+    *n = (uint32_t)E.tuning.size();
+    for (uint32_t i = 0; i < cap && i < E.tuning.size(); ++i)
+      e[i] = voss_gb300_tune_entry_t{E.tuning[i].b_max, E.tuning[i].width_max, E.tuning[i].seg_bytes,
+                                     E.tuning[i].tier_split};
     return VOSS_OK;
   }, VOSS_ERR_INTERNAL);
 }

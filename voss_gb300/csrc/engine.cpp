@@ -113,6 +113,12 @@ void Engine::init() {
   build_tiles();
   scratch.eng = this;
   scratch.device = device;
+  // the offset-regime table measured by voss_gb300/autotune.py on GB300
+  static const TuneEntry kBuiltin[] = {
+#include "tune_table.inc"
+  };
+  for (const TuneEntry& t : kBuiltin)
+    if (t.seg_bytes) tuning.push_back(t);
   ensure_table(65536);
 }
 
@@ -195,19 +201,24 @@ Config Engine::tuned_for(uint64_t a, uint64_t b, bool batch) const {
   if (!cfg.auto_tune) return c;
   const uint64_t width = b > a ? b - a : 0;
   const uint64_t bytes = width / 30 + 1;
+  // Offset regime: the table gives the largest segment and the tier split
+  // measured best for ranges ending below b_max and no wider than width_max.
+  uint32_t s = cfg.seg_bytes;
+  uint32_t split = 0;
   for (const TuneEntry& t : tuning) {
     if (b <= t.b_max && width <= t.width_max) {
-      c.seg_bytes = std::min<uint32_t>(std::max<uint32_t>(t.seg_bytes, 1024), cfg.seg_bytes) & ~127u;
-      c.tier_split = std::max<uint32_t>(kFirstTablePrime, t.tier_split);
-      return c;
+      s = std::min<uint32_t>(std::max<uint32_t>(t.seg_bytes, 1024), cfg.seg_bytes) & ~127u;
+      split = std::max<uint32_t>(kFirstTablePrime, t.tier_split);
+      break;
     }
   }
-  // Built-in rule.  Alone, a range should fill the GPU in whole waves: the
-  // segment is shrunk until the segments come in full waves of one CTA per
-  // SM (not below 16 KiB, where the per-prime setup dominates).  In a batch
-  // other ranges fill the GPU, so the largest segment is the cheapest.
-  uint32_t s = cfg.seg_bytes;
-  if (!batch) {
+  // Alone, a range should fill the GPU in whole waves: the segment shrinks
+  // until the segments come in full waves of one CTA per SM (not below 16 KiB,
+  // where the per-prime setup dominates).  In a batch other ranges fill the
+  // GPU, so the largest segment is the cheapest.
+  if (batch) {
+    s = cfg.seg_bytes;
+  } else {
     const uint64_t g = (uint64_t)sm_count * cfg.ctas_per_sm;
     const uint64_t waves = (bytes + g * s - 1) / (g * s);
     uint64_t want = (bytes + waves * g - 1) / (waves * g);
@@ -215,9 +226,10 @@ Config Engine::tuned_for(uint64_t a, uint64_t b, bool batch) const {
     s = (uint32_t)std::min<uint64_t>(s, (want + 127) & ~127ull);
   }
   c.seg_bytes = s;
-  // The warp-per-prime tier ends where a class has about 32 hits per
-  // segment (measured best on GB300 between 1e10 and 1e14).
-  c.tier_split = std::max<uint32_t>(kFirstTablePrime, std::min<uint32_t>(cfg.tier_split, s / 32));
+  // Without a table entry the warp-per-prime tier ends where a class has
+  // about 32 hits per segment.
+  c.tier_split = split ? split
+                       : std::max<uint32_t>(kFirstTablePrime, std::min<uint32_t>(cfg.tier_split, s / 32));
   return c;
 }
 

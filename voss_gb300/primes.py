@@ -273,6 +273,35 @@ def in_range_with_limit(a: int, b: int, max_count: int) -> list:
     return _array_result(rc, arr, cnt)
 
 
+def nth(n: int) -> int:
+    """The n-th prime, 1-indexed: nth(1) = 2 (n <= 5*10^7)."""
+    if not isinstance(n, int):
+        raise TypeError("n must be int")
+    if n < 1:
+        raise VossInvalidNError(f"n must be >= 1 (1-indexed), got {n}")
+    out = ctypes.c_uint64(0)
+    _capi._check(_capi._lib.voss_primes_nth(n, ctypes.byref(out)), _ERRMAP)
+    return out.value
+
+
+def next_prime(x: int) -> int:
+    """The smallest prime strictly greater than x."""
+    if not isinstance(x, int):
+        raise TypeError("x must be int")
+    out = ctypes.c_uint64(0)
+    _capi._check(_capi._lib.voss_primes_next(max(x, 0), ctypes.byref(out)), _ERRMAP)
+    return out.value
+
+
+def prev_prime(x: int) -> int:
+    """The largest prime strictly less than x."""
+    if not isinstance(x, int):
+        raise TypeError("x must be int")
+    out = ctypes.c_uint64(0)
+    _capi._check(_capi._lib.voss_primes_prev(max(x, 0), ctypes.byref(out)), _ERRMAP)
+    return out.value
+
+
 # ---------------------------------------------------------------------------
 # additive: statistics of arbitrary half-open ranges
 # ---------------------------------------------------------------------------
