@@ -87,6 +87,12 @@ typedef struct {
     uint32_t tier_split;
     uint32_t ctas_per_sm;
     uint32_t auto_tune;
+    uint32_t bucket_split;   /* with auto_tune = 0: primes from here on (and >= the
+                                segment) go through bucket lists; 0 = none */
+    uint32_t bucket_cap_pct; /* bucket list capacity in percent of the default
+                                (many standard deviations above the mean); a
+                                list that overflows makes the run repeat
+                                without lists, so results never change */
 } voss_gb300_config_t;
 
 int voss_gb300_get_config(voss_gb300_config_t* out);
@@ -95,12 +101,15 @@ int voss_gb300_set_config(const voss_gb300_config_t* cfg);
 /* Offset-regime tuning table (written by voss_gb300/autotune.py, a built-in
  * copy ships in the library): a range [a, b) uses the first entry with
  * b <= b_max and b - a <= width_max.  n = 0 clears the table (the built-in
- * rule then applies). */
+ * rule then applies).  Bucket lists are used for ranges of 2 to 4096
+ * segments. */
 typedef struct {
     uint64_t b_max;
     uint64_t width_max;
     uint32_t seg_bytes;
     uint32_t tier_split;
+    uint32_t bucket_split;   /* primes from here on (and >= the segment) are
+                                marked from per-segment bucket lists; 0 = none */
 } voss_gb300_tune_entry_t;
 
 int voss_gb300_set_tuning(uint32_t n, const voss_gb300_tune_entry_t* entries);
@@ -126,9 +135,10 @@ int voss_gb300_plan_info(voss_gb300_plan* plan, uint64_t* total_segments, uint32
                          uint32_t* kernels_per_run, uint32_t* smem_bytes,
                          uint64_t* clears, uint64_t* wheel_bytes);
 void voss_gb300_plan_free(voss_gb300_plan* plan);
-/* Durations in ms of the sieve kernel and the finalize kernel of the plan's
- * last launch, from CUDA events recorded on the launching stream (waits for
- * that launch to finish). */
+/* Durations in ms of the sieve (the bucket fill kernel, when the run uses
+ * bucket lists, plus the sieve kernel) and of the finalize kernel of the
+ * plan's last launch, from CUDA events recorded on the launching stream
+ * (waits for that launch to finish). */
 int voss_gb300_plan_kernel_ms(voss_gb300_plan* plan, float* sieve_ms, float* finalize_ms);
 
 /* Every even n in [4, N], N <= 4*10^11: the smallest prime p with n - p prime
@@ -157,7 +167,8 @@ void voss_gb300_goldbach_free(voss_gb300_goldbach* g);
  * pending ones into batches, FIFO, while batch slots and device memory
  * (segment records, accumulators, results of every batch in flight) allow,
  * and runs each batch as one replayed CUDA graph on its slot's stream, so
- * batches overlap on the device.  The reference has no counterpart: it
+ * batches overlap on the device.  Admission counts each request's segment
+ * records, accumulators, results and bucket lists.  The reference has no counterpart: it
  * serves one Context at a time (context.cu:212-559).  Every request gets the
  * full voss_range_stats_t; for COUNT and CHEBYSHEV requests the gap fields
  * are not computed (zero). */
@@ -172,6 +183,7 @@ typedef struct {
     uint64_t max_segments;        /* segments per batch (default 32768) */
     uint64_t memory_budget;       /* device bytes over all batches in flight */
     uint32_t use_graphs;          /* replay a captured CUDA graph per batch */
+    uint64_t bucket_bytes;        /* bucket-list arena per slot (default 256 MiB) */
 } voss_gb300_server_config_t;
 
 typedef struct {

@@ -292,3 +292,46 @@ def test_nth_next_prev(vg, oracle_lib):
     for k in (6, 7, 1234, 78498, 78499, 5761455, 50000000):
         p = vg.primes.nth(k)
         assert oracle_lib.range_stats(0, p + 1)["count"] == k and oracle_lib.range_stats(p, p + 1)["count"] == 1
+
+
+def _with_config(vg, **cfg):
+    base = vg.primes.get_config()
+    vg.primes.set_config(**cfg)
+    return base
+
+
+def test_bucket_lists_vs_oracle(vg, oracle_lib):
+    """Primes above the bucket split marked from per-segment lists."""
+    rng = random.Random(5)
+    cases = [(10**14, 10**14 + 2 * 10**7), (10**14 + 10**10 - 3 * 10**7, 10**14 + 10**10 + 1),
+             (10**13 - 10**7, 10**13 + 10**7), (10**12 + 12345, 10**12 + 12345 + 4 * 10**7)]
+    for _ in range(6):
+        a = rng.randrange(10**11, 10**14)
+        cases.append((a, a + rng.randrange(7 * 10**6, 5 * 10**7)))
+    want = [oracle_lib.range_stats(a, b) for a, b in cases]
+    for split in (221184, 442368):
+        base = _with_config(vg, seg_bytes=221184, tier_split=4096, bucket_split=split, auto_tune=0)
+        try:
+            for (a, b), w in zip(cases, want):
+                assert_range_equal(vg.range_stats(a, b, full=True), w, (split, a, b))
+            res = vg.range_stats_batch(cases)
+            for r, w in zip(res, want):
+                assert r.count == w["count"] and r.max_gap == w["max_gap"] and r.twins == int(w["hist"][1])
+        finally:
+            vg.primes.set_config(**base)
+
+
+def test_bucket_overflow_falls_back(vg, oracle_lib):
+    """Lists far too small for their hits: the run repeats without lists."""
+    a, b = 10**14, 10**14 + 3 * 10**7
+    want = oracle_lib.range_stats(a, b)
+    base = _with_config(vg, seg_bytes=221184, tier_split=4096, bucket_split=221184, bucket_cap_pct=1,
+                        auto_tune=0)
+    try:
+        assert_range_equal(vg.range_stats(a, b, full=True), want, "overflow")
+        from voss_gb300.serve import Server
+        with Server(slots=1) as srv:
+            got, _ = srv.result(srv.submit(a, b, 2))
+            assert got.count == want["count"] and got.max_gap == want["max_gap"]
+    finally:
+        vg.primes.set_config(**base)

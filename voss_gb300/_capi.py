@@ -69,7 +69,8 @@ class VossRangeStats(ctypes.Structure):
 
 class VossConfig(ctypes.Structure):
     _fields_ = [("seg_bytes", u32), ("threads", u32), ("tier_split", u32),
-                ("ctas_per_sm", u32), ("auto_tune", u32)]
+                ("ctas_per_sm", u32), ("auto_tune", u32), ("bucket_split", u32),
+                ("bucket_cap_pct", u32)]
 
 
 PROGRESS_CB = ctypes.CFUNCTYPE(None, c_int, c_int, u64, u64, vp)

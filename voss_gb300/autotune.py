@@ -37,11 +37,13 @@ REGIMES = [
 ]
 SEGS = [65536, 98304, 131072, 163840, 196608, 221184]
 SPLITS = [1024, 2048, 4096, 6144, 12288]
+BUCKETS = [0, 221184, 442368, 884736, 1769472]   # bucket-list split (0 = none)
 
 
 class TuneEntry(ctypes.Structure):
     _fields_ = [("b_max", ctypes.c_uint64), ("width_max", ctypes.c_uint64),
-                ("seg_bytes", ctypes.c_uint32), ("tier_split", ctypes.c_uint32)]
+                ("seg_bytes", ctypes.c_uint32), ("tier_split", ctypes.c_uint32),
+                ("bucket_split", ctypes.c_uint32)]
 
 
 def set_table(lib, entries):
@@ -73,28 +75,36 @@ def run(quick=False, write=False, out=sys.stdout):
     stream = torch.cuda.Stream()
     segs = SEGS[-3:] if quick else SEGS
     splits = SPLITS[1:4] if quick else SPLITS
+    buckets = BUCKETS[:3] if quick else BUCKETS
     table = []
     for b_max, w_max, ranges in REGIMES:
         best = None
         for sb in segs:
             for sp in splits:
-                set_table(lib, [(U64_MAX, U64_MAX, sb, sp)])
+                set_table(lib, [(U64_MAX, U64_MAX, sb, sp, 0)])
                 t = sum(time_range(SievePlan, stream, a, b, 3) for a, b in ranges)
                 if best is None or t < best[0]:
-                    best = (t, sb, sp)
-        table.append((b_max, w_max, best[1], best[2]))
+                    best = (t, sb, sp, 0)
+        # then the bucket split at the best segment and tier split
+        for bk in buckets[1:]:
+            set_table(lib, [(U64_MAX, U64_MAX, best[1], best[2], bk)])
+            t = sum(time_range(SievePlan, stream, a, b, 3) for a, b in ranges)
+            if t < best[0]:
+                best = (t, best[1], best[2], bk)
+        table.append((b_max, w_max, best[1], best[2], best[3]))
         print(f"b <= {b_max:.3g}, width <= {w_max:.3g}: seg_bytes={best[1]} tier_split={best[2]} "
-              f"({best[0]:.3f} ms over {len(ranges)} ranges)", file=out, flush=True)
+              f"bucket_split={best[3]} ({best[0]:.3f} ms over {len(ranges)} ranges)", file=out, flush=True)
     set_table(lib, table)
     if write:
-        lines = ["// Offset-regime tuning table: {b_max, width_max, seg_bytes, tier_split}.",
+        lines = ["// Offset-regime tuning table: {b_max, width_max, seg_bytes, tier_split, bucket_split, 0}.",
                  "// Written by voss_gb300/autotune.py from timings on a GB300; the built-in",
                  "// wave rule of Engine::tuned_for applies on top of seg_bytes."]
-        for b_max, w_max, sb, sp in table:
-            lines.append("{%dull, %dull, %d, %d}," % (b_max, w_max, sb, sp))
+        for b_max, w_max, sb, sp, bk in table:
+            lines.append("{%dull, %dull, %d, %d, %d, 0}," % (b_max, w_max, sb, sp, bk))
         (HERE / "csrc" / "tune_table.inc").write_text("\n".join(lines) + "\n")
         (HERE / "tune_table.json").write_text(json.dumps(
-            [dict(b_max=b, width_max=w, seg_bytes=s, tier_split=t) for b, w, s, t in table], indent=1) + "\n")
+            [dict(b_max=b, width_max=w, seg_bytes=s, tier_split=t, bucket_split=k)
+             for b, w, s, t, k in table], indent=1) + "\n")
     return table
 
 

@@ -640,6 +640,8 @@ extern "C" int voss_gb300_get_config(voss_gb300_config_t* out) {
     out->tier_split = E.cfg.tier_split;
     out->ctas_per_sm = E.cfg.ctas_per_sm;
     out->auto_tune = E.cfg.auto_tune;
+    out->bucket_split = E.cfg.bucket_split;
+    out->bucket_cap_pct = E.cfg.bucket_cap_pct;
     return VOSS_OK;
   }, VOSS_ERR_INTERNAL);
 }
@@ -668,6 +670,8 @@ extern "C" int voss_gb300_set_config(const voss_gb300_config_t* c) {
     if (c->tier_split) n.tier_split = c->tier_split;
     if (c->ctas_per_sm) n.ctas_per_sm = c->ctas_per_sm;
     n.auto_tune = c->auto_tune ? 1 : 0;
+    n.bucket_split = c->bucket_split;
+    if (c->bucket_cap_pct) n.bucket_cap_pct = c->bucket_cap_pct;
     if (vg::sieve_smem_bytes(n.seg_bytes, n.threads) > E.max_smem_optin)
       throw vg::Error(VOSS_ERR_INVALID_ARG, "segment does not fit in shared memory");
     E.cfg = n;
@@ -688,7 +692,8 @@ extern "C" int voss_gb300_set_tuning(uint32_t n, const voss_gb300_tune_entry_t* 
     std::lock_guard<std::mutex> g(E.mu);
     E.tuning.clear();
     for (uint32_t i = 0; i < n; ++i)
-      E.tuning.push_back(vg::TuneEntry{e[i].b_max, e[i].width_max, e[i].seg_bytes, e[i].tier_split});
+      E.tuning.push_back(vg::TuneEntry{e[i].b_max, e[i].width_max, e[i].seg_bytes, e[i].tier_split,
+                                       e[i].bucket_split, 0});
     return VOSS_OK;
   }, VOSS_ERR_INTERNAL);
 }
@@ -701,7 +706,7 @@ extern "C" int voss_gb300_get_tuning(uint32_t cap, voss_gb300_tune_entry_t* e, u
     *n = (uint32_t)E.tuning.size();
     for (uint32_t i = 0; i < cap && i < E.tuning.size(); ++i)
       e[i] = voss_gb300_tune_entry_t{E.tuning[i].b_max, E.tuning[i].width_max, E.tuning[i].seg_bytes,
-                                     E.tuning[i].tier_split};
+                                     E.tuning[i].tier_split, E.tuning[i].bucket_split};
     return VOSS_OK;
   }, VOSS_ERR_INTERNAL);
 }
@@ -759,7 +764,8 @@ extern "C" int voss_gb300_plan_info(voss_gb300_plan* p, uint64_t* total_segments
   return guarded([&] {
     if (total_segments) *total_segments = p->plan.total_segs;
     if (grid) *grid = p->plan.grid;
-    if (kernels_per_run) *kernels_per_run = p->plan.nreq ? vg::Plan::kKernels : 0;
+    if (kernels_per_run)
+      *kernels_per_run = p->plan.nreq ? vg::Plan::kKernels + (p->plan.nfill ? 1u : 0u) : 0;
     if (smem_bytes) *smem_bytes = (uint32_t)vg::sieve_smem_bytes(p->plan.seg_max, p->plan.threads);
     if (clears) *clears = p->plan.algorithmic_clears();
     if (wheel_bytes) *wheel_bytes = p->plan.wheel_bytes();
@@ -878,6 +884,7 @@ extern "C" int voss_gb300_server_create(const voss_gb300_server_config_t* c, vos
       if (c->max_batch) sc.max_batch = c->max_batch;
       if (c->max_segments) sc.max_segs = c->max_segments;
       if (c->memory_budget) sc.mem_budget = c->memory_budget;
+      if (c->bucket_bytes) sc.bucket_bytes = c->bucket_bytes;
       sc.use_graphs = c->use_graphs;
     }
     vg::Engine& E = vg::Engine::for_current_device();

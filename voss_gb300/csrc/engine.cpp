@@ -181,6 +181,8 @@ void Engine::ensure_table(uint64_t pmax) {
     check_cuda(cudaMemcpy(dR.ptr, R.data(), R.size() * 4, cudaMemcpyHostToDevice), "table R");
   }
   rstride = stride;
+  hInvPrefix.assign(n + 1, 0.0);
+  for (size_t i = 0; i < n; ++i) hInvPrefix[i + 1] = hInvPrefix[i] + 1.0 / (double)P[i];
   hP.swap(P);
   table_limit = lim;
 }
@@ -205,10 +207,12 @@ Config Engine::tuned_for(uint64_t a, uint64_t b, bool batch) const {
   // measured best for ranges ending below b_max and no wider than width_max.
   uint32_t s = cfg.seg_bytes;
   uint32_t split = 0;
+  c.bucket_split = 0;
   for (const TuneEntry& t : tuning) {
     if (b <= t.b_max && width <= t.width_max) {
       s = std::min<uint32_t>(std::max<uint32_t>(t.seg_bytes, 1024), cfg.seg_bytes) & ~127u;
       split = std::max<uint32_t>(kFirstTablePrime, t.tier_split);
+      c.bucket_split = t.bucket_split;
       break;
     }
   }
@@ -233,18 +237,57 @@ Config Engine::tuned_for(uint64_t a, uint64_t b, bool batch) const {
   return c;
 }
 
+BucketPlan Engine::bucket_plan(const Config& c, uint64_t b, uint32_t nprimes, uint64_t nseg,
+                               uint32_t seg_bytes) const {
+  BucketPlan bp{nprimes, 0};
+  // Lists pay off when most (prime, segment) pairs have no hit: primes well
+  // above the segment, a request of several segments (one fill pass replaces
+  // a setup per prime per segment), few enough segments for the fill
+  // kernel's shared counts.
+  if (!c.bucket_split || nseg < 2 || nseg > kMaxBucketSegs || b < 2) return bp;
+  const uint32_t from = std::max<uint32_t>(c.bucket_split, seg_bytes);
+  const uint32_t idx = index_of(from);
+  if (idx >= nprimes) return bp;
+  // expected entries per segment: 8 * S * sum(1/p) over the bucket primes;
+  // the capacity leaves a margin of many standard deviations
+  const double mean = 8.0 * seg_bytes * (hInvPrefix[nprimes] - hInvPrefix[idx]);
+  const double cap = (mean * 1.25 + 32.0 * std::sqrt(mean) + 1024.0) * cfg.bucket_cap_pct / 100.0;
+  bp.bucket_idx = idx;
+  bp.cap = std::max<uint32_t>(32u, ((uint32_t)cap + 31u) & ~31u);
+  return bp;
+}
+
 // ---------------------------------------------------------------------------
 // Plan
 // ---------------------------------------------------------------------------
-void Plan::reserve_capacity(uint32_t max_req, uint64_t max_segs) {
+void Plan::reserve_capacity(uint32_t max_req, uint64_t max_segs, uint64_t max_bucket_entries) {
   cap_req = std::max<uint32_t>(max_req, 1);
   cap_segs = std::max<uint64_t>(max_segs, 1);
+  cap_bucket = max_bucket_entries;
+  cap_fill = max_bucket_entries ? 65536u : 0u;
+  if (cap_bucket) bucket.reserve(4 * cap_bucket);
+  if (cap_fill) fills.reserve(sizeof(FillItem) * cap_fill);
+  bcount.reserve(4 * cap_segs);
   reqs.reserve(sizeof(ReqDesc) * cap_req);
   segs.reserve(sizeof(SegRec) * cap_segs);
   acc.reserve(sizeof(ReqAccum) * cap_req);
   results.reserve(sizeof(ReqResult) * cap_req);
   stage.reserve(sizeof(BatchHdr) + sizeof(ReqDesc) * cap_req);
   host_results.reserve(sizeof(ReqResult) * cap_req);
+}
+
+uint64_t Plan::bucket_bytes_for(uint64_t a, uint64_t b) const {
+  if (b <= a || !allow_buckets) return 0;
+  Engine& E = *eng;
+  const Config c = E.tuned_for(a, b, batch_mode);
+  const uint64_t bytes = (b + 29) / 30 - a / 30;
+  const uint64_t nseg = (bytes + c.seg_bytes - 1) / c.seg_bytes;
+  const BucketPlan bp = E.bucket_plan(c, b, E.primes_below_sq(b), nseg, c.seg_bytes);
+  return bp.cap ? 4ull * bp.cap * nseg : 0;
+}
+
+bool Plan::overflowed() const {
+  return nfill && host_flag.ptr && *static_cast<const unsigned int*>(host_flag.ptr) != 0;
 }
 
 uint64_t Plan::segments_for(uint64_t a, uint64_t b) const {
@@ -299,13 +342,35 @@ void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
                      [](const Item& x, const Item& y) { return x.cost > y.cost; });
   host_reqs.resize(n);
   order.resize(n);
-  uint64_t base = 0;
+  host_fills.clear();
+  uint64_t base = 0, bbase = 0;
   for (uint32_t i = 0; i < n; ++i) {
-    host_reqs[i] = items[i].d;
-    host_reqs[i].seg_base = base;
+    ReqDesc& r = host_reqs[i];
+    r = items[i].d;
+    r.seg_base = base;
+    r.bucket_idx = r.nprimes;
+    r.bucket_base = 0;
+    r.bucket_cap = 0;
     order[i] = items[i].idx;
-    base += host_reqs[i].nseg;
+    base += r.nseg;
+    if (allow_buckets && r.nseg && !(fl & kFlagBitmap)) {
+      const Config c = E.tuned_for(r.a, r.b, many);
+      const BucketPlan bp = E.bucket_plan(c, r.b, r.nprimes, r.nseg, r.seg_bytes);
+      const uint64_t need = (uint64_t)bp.cap * r.nseg;
+      const uint64_t items_need = (r.nprimes - bp.bucket_idx + kFillPrimes - 1) / kFillPrimes;
+      const bool fits = !cap_req || (bbase + need <= cap_bucket && host_fills.size() + items_need <= cap_fill);
+      if (bp.cap && fits) {
+        r.bucket_idx = bp.bucket_idx;
+        r.bucket_cap = bp.cap;
+        r.bucket_base = bbase;
+        bbase += need;
+        for (uint32_t p0 = bp.bucket_idx; p0 < r.nprimes; p0 += kFillPrimes)
+          host_fills.push_back(FillItem{i, p0, std::min<uint32_t>(p0 + kFillPrimes, r.nprimes), 0});
+      }
+    }
   }
+  bucket_entries = bbase;
+  nfill = (uint32_t)host_fills.size();
   nreq = n;
   total_segs = base;
   if (cap_req) {
@@ -325,6 +390,12 @@ void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
     const uint64_t words = (host_reqs[0].k_hi - host_reqs[0].k_lo + 3) / 4 + 1;
     bitmap.reserve(words * 4);
   }
+  if (!cap_req) {
+    bucket.reserve(4 * std::max<uint64_t>(bucket_entries, 1));
+    fills.reserve(sizeof(FillItem) * std::max<uint32_t>(nfill, 1));
+    bcount.reserve(4 * std::max<uint64_t>(total_segs, 1));
+  }
+  overflow.reserve(sizeof(unsigned int));
   hdr.reserve(sizeof(BatchHdr));
   queue.reserve(sizeof(unsigned long long));
   large.reserve(sizeof(LargeGapRec) * large_cap);
@@ -332,7 +403,7 @@ void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
   BatchHdr* h = static_cast<BatchHdr*>(stage.ptr);
   h->total_segs = total_segs;
   h->nreq = nreq;
-  h->pad = 0;
+  h->nfill = nfill;
   if (n) std::memcpy(h + 1, host_reqs.data(), sizeof(ReqDesc) * n);
   const uint64_t gcap = (uint64_t)E.sm_count * E.cfg.ctas_per_sm;
   grid = (uint32_t)(cap_req ? gcap : std::min<uint64_t>(total_segs, gcap));
@@ -354,6 +425,8 @@ void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
   prm.large_cap = large_cap;
   prm.flags = flags;
   prm.bitmap = bitmap.as<uint32_t>();
+  prm.bucket = bucket.as<uint32_t>();
+  prm.bcount = bcount.as<uint32_t>();
 }
 
 void Plan::prepare(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl) {
@@ -368,6 +441,9 @@ void Plan::upload(cudaStream_t s) {
     check_cuda(cudaMemcpyAsync(reqs.ptr, static_cast<const char*>(stage.ptr) + sizeof(BatchHdr),
                                bytes - sizeof(BatchHdr), cudaMemcpyHostToDevice, s),
                "upload requests");
+  if (nfill)
+    check_cuda(cudaMemcpyAsync(fills.ptr, host_fills.data(), sizeof(FillItem) * nfill,
+                               cudaMemcpyHostToDevice, s), "upload fill items");
 }
 
 Plan::~Plan() {
@@ -415,7 +491,28 @@ void Plan::run_device(cudaStream_t s) {
   check_cuda(cudaMemsetAsync(acc.ptr, 0, sizeof(ReqAccum) * nacc, s), "memset accumulators");
   check_cuda(cudaMemsetAsync(nlarge.ptr, 0, sizeof(unsigned int), s), "memset large count");
   check_cuda(cudaMemsetAsync(queue.ptr, 0, sizeof(unsigned long long), s), "memset work queue");
+  check_cuda(cudaMemsetAsync(overflow.ptr, 0, sizeof(unsigned int), s), "memset overflow");
+  const uint64_t nsegs_dev = cap_req ? cap_segs : total_segs;
+  if (nsegs_dev)
+    check_cuda(cudaMemsetAsync(bcount.ptr, 0, 4 * nsegs_dev, s), "memset bucket counts");
+  // the sieve's timed span covers the bucket fill that feeds it
   check_cuda(cudaEventRecord(ev[0], s), "event");
+  if (cap_req ? cap_fill : nfill) {
+    FillParams fp;
+    fp.reqs = reqs.as<ReqDesc>();
+    fp.hdr = hdr.as<BatchHdr>();
+    fp.items = fills.as<FillItem>();
+    fp.P = prm.P;
+    fp.M = prm.M;
+    fp.R = prm.R;
+    fp.rstride = prm.rstride;
+    fp.bucket = bucket.as<uint32_t>();
+    fp.bcount = bcount.as<uint32_t>();
+    fp.overflow = overflow.as<unsigned int>();
+    const uint32_t fgrid = cap_req ? eng->sm_count * 4
+                                   : (uint32_t)std::min<uint64_t>(nfill, (uint64_t)eng->sm_count * 4);
+    check_cuda(launch_bucket_fill(fp, fgrid, s), "bucket_fill_kernel");
+  }
   check_cuda(launch_sieve(prm, grid, threads, s), "sieve_segments_kernel");
   check_cuda(cudaEventRecord(ev[1], s), "event");
   check_cuda(launch_finalize(reqs.as<ReqDesc>(), hdr.as<BatchHdr>(), segs.as<SegRec>(),
@@ -429,6 +526,11 @@ void Plan::fetch_async(cudaStream_t s) {
   if (nreq)
     check_cuda(cudaMemcpyAsync(host_results.ptr, results.ptr, sizeof(ReqResult) * nreq,
                                cudaMemcpyDeviceToHost, s), "download results");
+  if (nfill) {
+    host_flag.reserve(sizeof(unsigned int));
+    check_cuda(cudaMemcpyAsync(host_flag.ptr, overflow.ptr, sizeof(unsigned int),
+                               cudaMemcpyDeviceToHost, s), "download overflow flag");
+  }
 }
 
 const ReqResult* Plan::finish() {
@@ -492,9 +594,17 @@ uint64_t Plan::algorithmic_clears() const {
 const ReqResult* Engine::run(uint32_t n, const uint64_t* a, const uint64_t* b,
                              std::vector<LargeGapRec>* lg, bool gaps) {
   std::vector<uint32_t> rf(n, gaps ? kReqGaps : 0u);
+  scratch.allow_buckets = true;
   scratch.load(n, a, b, 0, rf.data());
   scratch.launch(stream);
   const ReqResult* r = scratch.fetch(stream);
+  if (scratch.overflowed()) {                // a bucket list ran out of room: redo without lists
+    scratch.allow_buckets = false;
+    scratch.load(n, a, b, 0, rf.data());
+    scratch.launch(stream);
+    scratch.allow_buckets = true;
+    r = scratch.fetch(stream);
+  }
   if (lg) *lg = scratch.fetch_large(stream);
   return r;
 }

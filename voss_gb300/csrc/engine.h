@@ -56,6 +56,8 @@ struct Config {
   uint32_t tier_split = 6144;    // primes below: a warp per prime; above: 4 per warp
   uint32_t ctas_per_sm = 1;
   uint32_t auto_tune = 1;
+  uint32_t bucket_split = 0;   // with auto_tune off: bucket primes from here (0 = none)
+  uint32_t bucket_cap_pct = 100;   // bucket list capacity, percent of the safe size
 };
 
 class Engine;
@@ -83,8 +85,16 @@ struct Plan {
   std::vector<ReqDesc> host_reqs;   // device order
   std::vector<uint32_t> order;      // host_reqs[i] is the caller's request order[i]
   DevBuf reqs, hdr, queue, segs, acc, large, nlarge, results, bitmap;
+  DevBuf bucket, bcount, fills, overflow;   // bucket sieve lists, per-segment counts, fill items
+  uint64_t bucket_entries = 0;  // entries reserved by the current batch
+  uint64_t cap_bucket = 0;      // fixed arena (graph-replayed plans); 0 = exact
+  uint32_t nfill = 0;
+  uint32_t cap_fill = 0;
+  bool allow_buckets = true;
+  std::vector<FillItem> host_fills;
   HostPinned stage;             // BatchHdr followed by ReqDesc[cap]
   HostPinned host_results;      // ReqResult[] in device order
+  HostPinned host_flag;         // the overflow flag, copied with the results
   std::vector<ReqResult> out;   // caller order
   uint32_t large_cap = 1u << 16;
   uint32_t flags = 0;
@@ -99,8 +109,9 @@ struct Plan {
   // Kernels per run (sieve + finalize).
   static constexpr uint32_t kKernels = 2;
 
-  // Fix the capacity (requests, segments) of a graph-replayed plan.
-  void reserve_capacity(uint32_t max_req, uint64_t max_segs);
+  // Fix the capacity (requests, segments, bucket entries) of a
+  // graph-replayed plan.
+  void reserve_capacity(uint32_t max_req, uint64_t max_segs, uint64_t max_bucket_entries = 0);
   // rflags: per request kReqGaps (NULL = all requests want gaps)
   void load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t flags,
             const uint32_t* rflags = nullptr);
@@ -128,6 +139,18 @@ struct Plan {
   void kernel_ms(float* sieve_ms, float* finalize_ms);
   // Segments a range needs under this plan's tuning (for admission).
   uint64_t segments_for(uint64_t a, uint64_t b) const;
+  // Bucket-list bytes a range needs under this plan's tuning (for admission).
+  uint64_t bucket_bytes_for(uint64_t a, uint64_t b) const;
+  // True if the last run's bucket lists overflowed (its results are then
+  // invalid); valid once the stream has passed fetch_async().
+  bool overflowed() const;
+};
+
+// Bucket layout of one request: first bucket prime, list capacity per
+// segment.  bucket_idx = nprimes when the request does not use buckets.
+struct BucketPlan {
+  uint32_t bucket_idx;
+  uint32_t cap;
 };
 
 // One entry of the offset-regime tuning table: ranges with b <= b_max and
@@ -137,6 +160,8 @@ struct TuneEntry {
   uint64_t width_max;
   uint32_t seg_bytes;
   uint32_t tier_split;
+  uint32_t bucket_split;   // primes from here on go through bucket lists; 0 = none
+  uint32_t pad;
 };
 
 class Engine {
@@ -153,6 +178,7 @@ class Engine {
 
   // Resident sieving-prime table: primes >= 37 up to table_limit.
   std::vector<uint32_t> hP;
+  std::vector<double> hInvPrefix;   // sum of 1/p over table primes [0, i)
   uint64_t table_limit = 0;
   DevBuf dP, dM, dR;
   uint64_t rstride = 0;
@@ -168,6 +194,9 @@ class Engine {
   // built-in rule); batch = tune for the throughput of a batch rather than
   // the latency of this range alone.
   Config tuned_for(uint64_t a, uint64_t b, bool batch = false) const;
+  // Bucket layout for a range with the given segment size and segment count.
+  BucketPlan bucket_plan(const Config& c, uint64_t b, uint32_t nprimes, uint64_t nseg,
+                         uint32_t seg_bytes) const;
   std::vector<TuneEntry> tuning;
 
   // Run ranges synchronously on the engine stream.
@@ -188,6 +217,7 @@ void to_public(const ReqResult& r, uint64_t a, uint64_t b, voss_range_stats_t* o
 size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads);
 cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads,
                          cudaStream_t stream);
+cudaError_t launch_bucket_fill(const FillParams& fp, uint32_t grid, cudaStream_t stream);
 cudaError_t launch_finalize(const ReqDesc* reqs, const BatchHdr* hdr, const SegRec* segs,
                             ReqAccum* acc, LargeGapRec* large, unsigned int* n_large,
                             uint32_t large_cap, ReqResult* out, uint32_t grid,

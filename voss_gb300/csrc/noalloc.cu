@@ -171,7 +171,7 @@ __global__ void na_init_kernel(NaScratch* s, ReqDesc r) {
   if (threadIdx.x == 0) {
     s->hdr.total_segs = r.nseg;
     s->hdr.nreq = 1;
-    s->hdr.pad = 0;
+    s->hdr.nfill = 0;
     s->queue = 0;
     s->nlarge = 0;
     s->req = r;
@@ -240,6 +240,7 @@ extern "C" int voss_primes_range_stats_noalloc(uint64_t a, uint64_t b, voss_rang
     r.tier_split = (uint32_t)(std::lower_bound(h_P, h_P + kNaPrimes, split) - h_P);
     r.tier_huge = (uint32_t)(std::lower_bound(h_P, h_P + kNaPrimes, r.seg_bytes) - h_P);
   }
+  r.bucket_idx = r.nprimes;          // no bucket lists on this path
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   NaScratch* sc = d.scratch;
   na_init_kernel<<<1, 256, 0, s>>>(sc, r);

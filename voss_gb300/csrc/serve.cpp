@@ -50,7 +50,7 @@ Server::Server(Engine& e, const ServerConfig& c) : E(e), cfg(c) {
     s.plan.eng = &E;
     s.plan.device = E.device;
     s.plan.batch_mode = true;
-    s.plan.reserve_capacity(cfg.max_batch, cfg.max_segs);
+    s.plan.reserve_capacity(cfg.max_batch, cfg.max_segs, cfg.bucket_bytes / 4);
     check_cuda(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "server stream");
     check_cuda(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "server event");
   }
@@ -84,7 +84,10 @@ uint64_t Server::submit(uint64_t a, uint64_t b, uint32_t op) {
   t.b = b;
   t.op = op;
   t.segs = segs;
-  t.bytes = request_bytes(segs);
+  // bucket lists that do not fit a slot's arena are not used (the plan skips them)
+  uint64_t bb = slots[0]->plan.bucket_bytes_for(a, b);
+  if (bb > cfg.bucket_bytes) bb = 0;
+  t.bytes = request_bytes(segs) + bb;
   t.t_submit = now_us();
   uint64_t id;
   {
@@ -168,7 +171,20 @@ void Server::retire(Slot& s) {
   if (q != cudaSuccess) {
     err = std::string("batch failed: ") + cudaGetErrorString(q);
   } else {
-    r = s.plan.finish();
+    try {
+      if (s.plan.overflowed()) {              // a bucket list ran out of room: redo without lists
+        s.plan.allow_buckets = false;
+        s.plan.load((uint32_t)s.a.size(), s.a.data(), s.b.data(), 0, s.rf.data());
+        s.plan.upload(s.stream);
+        s.plan.run_device(s.stream);
+        s.plan.fetch(s.stream);
+        s.plan.allow_buckets = true;
+      }
+      r = s.plan.finish();
+    } catch (const std::exception& e) {
+      err = e.what();
+      s.plan.allow_buckets = true;
+    }
   }
   const double t = now_us();
   std::lock_guard<std::mutex> g(mu);
@@ -191,8 +207,12 @@ void Server::retire(Slot& s) {
 }
 
 bool Server::admit(Slot& s) {
-  std::vector<uint64_t> a, b;
-  std::vector<uint32_t> rf;
+  std::vector<uint64_t>& a = s.a;
+  std::vector<uint64_t>& b = s.b;
+  std::vector<uint32_t>& rf = s.rf;
+  a.clear();
+  b.clear();
+  rf.clear();
   uint64_t segs = 0, bytes = 0;
   {
     std::lock_guard<std::mutex> g(mu);

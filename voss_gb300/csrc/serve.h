@@ -25,6 +25,7 @@ struct ServerConfig {
   uint64_t max_segs = 1u << 15;  // segments per batch
   uint64_t mem_budget = 1ull << 30;   // device bytes over all batches in flight
   uint32_t use_graphs = 1;
+  uint64_t bucket_bytes = 256ull << 20;   // bucket-list arena per slot
 };
 
 class Server {
@@ -54,6 +55,8 @@ class Server {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     std::vector<uint64_t> ids;
+    std::vector<uint64_t> a, b;     // the batch, kept for a rerun without bucket lists
+    std::vector<uint32_t> rf;
     uint64_t bytes = 0;
     bool busy = false;
   };

@@ -110,7 +110,8 @@ sieve_segments_kernel(const SieveParams prm) {
   WarpRec* wrec = reinterpret_cast<WarpRec*>(shist + kSmemHistCopies * kSmemStride);
 
   __shared__ uint64_t s_k0, s_seg_in_req, s_item;
-  __shared__ uint32_t s_req, s_nbytes, s_np, s_ctr, s_split, s_huge, s_rflags;
+  __shared__ uint32_t s_req, s_nbytes, s_np, s_ctr, s_split, s_huge, s_rflags, s_bcnt;
+  __shared__ uint64_t s_bbase;
   __shared__ uint32_t s_vtab[32];      // bit b of a word -> 30*(b/8) + W30[b%8]
 
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -150,6 +151,13 @@ sieve_segments_kernel(const SieveParams prm) {
         const uint32_t mid = (a + b) >> 1;
         const uint64_t p = prm.P[mid];
         if (p * p < hi_num) a = mid + 1; else b = mid;
+      }
+      // primes from bucket_idx on come from this segment's bucket list
+      s_bcnt = 0;
+      if (R.bucket_idx < a) {
+        a = R.bucket_idx;
+        s_bcnt = min(prm.bcount[item], R.bucket_cap);
+        s_bbase = R.bucket_base + si * (uint64_t)R.bucket_cap;
       }
       s_req = lo; s_k0 = k0; s_seg_in_req = si; s_nbytes = nb; s_np = a;
     }
@@ -194,7 +202,10 @@ sieve_segments_kernel(const SieveParams prm) {
       const uint32_t nsmall = s_split < np ? s_split : np;
       const uint32_t hbeg = s_huge < np ? max(s_huge, nsmall) : np;
       const uint32_t nmidu = (hbeg - nsmall + 31u) / 32u;
-      const uint32_t nunits = nsmall + nmidu + (np - hbeg + 31u) / 32u;
+      const uint32_t nhugeu = (np - hbeg + 31u) / 32u;
+      const uint32_t nscan = nsmall + nmidu + nhugeu;
+      const uint32_t bcnt = s_bcnt;
+      const uint32_t nunits = nscan + (bcnt + kBucketUnit - 1) / kBucketUnit;
       const uint32_t o = lane & 7u, h = lane >> 3;
       for (;;) {
         uint32_t u = 0;
@@ -215,6 +226,16 @@ sieve_segments_kernel(const SieveParams prm) {
             uint32_t w = j0 >> 2;
 #pragma unroll 4
             for (; w < lim; w += p) atomicAnd(seg + w, mask);
+          }
+        } else if (u >= nscan) {
+          // bucket list of this segment: primes >= the bucket split whose
+          // hits were listed by bucket_fill_kernel; entries read coalesced
+          const uint64_t base = s_bbase + (uint64_t)(u - nscan) * kBucketUnit;
+          const uint32_t lim = min(kBucketUnit, bcnt - (u - nscan) * kBucketUnit);
+#pragma unroll 4
+          for (uint32_t e = lane; e < lim; e += 32) {
+            const uint32_t v = __ldg(prm.bucket + base + e);
+            clear_bit(seg, v & 0x3FFFFu, v >> 18);
           }
         } else if (u >= nsmall + nmidu) {
           // huge tier: p >= S, at most one hit per class; a lane per prime,
@@ -472,6 +493,78 @@ finalize_kernel(const ReqDesc* __restrict__ reqs, const BatchHdr* __restrict__ h
   }
 }
 
+// Bucket fill: one CTA per work item (a request and a run of its bucket
+// primes).  Pass 1 counts the hits of every prime (thread per prime, all eight
+// classes) per segment in shared memory; one global atomic per segment then
+// reserves room in that segment's list; pass 2 recomputes the hits and writes
+// the entries.  A list that would overflow its capacity raises *overflow and
+// drops the entry (the host then reruns without buckets).
+__global__ void __launch_bounds__(kFillPrimes)
+bucket_fill_kernel(const FillParams fp) {
+  __shared__ uint32_t cnt[kMaxBucketSegs];
+  __shared__ uint32_t gbase[kMaxBucketSegs];
+  const uint32_t tid = threadIdx.x;
+  const uint32_t nitems = fp.hdr->nfill;
+  for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const FillItem item = fp.items[it];
+    const ReqDesc R = fp.reqs[item.req];
+    const uint32_t nseg = (uint32_t)R.nseg;
+    const uint32_t S = R.seg_bytes;
+    const uint64_t k0 = R.k_lo;
+    const uint32_t total = (uint32_t)(R.k_hi - R.k_lo);
+    const float inv_s = 1.0f / (float)S;
+    for (uint32_t i = tid; i < nseg; i += blockDim.x) cnt[i] = 0;
+    __syncthreads();
+    const uint32_t i = item.p0 + tid;
+    const bool valid = i < item.p1;
+    uint32_t p = 0, m = 0;
+    bool low = false;
+    if (valid) {
+      p = __ldg(fp.P + i);
+      m = mod_barrett(k0, p, __ldg(fp.M + i));
+      low = 30ull * k0 < (uint64_t)p * p;
+    }
+    // segment of byte k: float estimate of k / S, corrected by one step
+    auto seg_of = [&](uint32_t k, uint32_t& off) {
+      uint32_t q = __float2uint_rz((float)k * inv_s);
+      int64_t r = (int64_t)k - (int64_t)q * S;
+      if (r < 0) { --q; r += S; } else if (r >= S) { ++q; r -= S; }
+      off = (uint32_t)r;
+      return q;
+    };
+    for (int pass = 0; pass < 2; ++pass) {
+      if (valid) {
+#pragma unroll 1
+        for (uint32_t o = 0; o < 8; ++o) {
+          const uint32_t r = __ldg(fp.R + o * fp.rstride + i);
+          uint32_t s = r >= m ? r - m : r + p - m;
+          if (low) s = lift_to_square(s, k0, p, o, total);
+          for (uint32_t k = s; k < total; k += p) {
+            uint32_t off;
+            const uint32_t sg = seg_of(k, off);
+            if (pass == 0) {
+              atomicAdd(&cnt[sg], 1u);
+            } else {
+              const uint32_t pos = gbase[sg] + atomicAdd(&cnt[sg], 1u);
+              if (pos < R.bucket_cap) fp.bucket[R.bucket_base + (uint64_t)sg * R.bucket_cap + pos] = bucket_entry(off, o);
+              else atomicOr(fp.overflow, 1u);
+            }
+          }
+        }
+      }
+      __syncthreads();
+      if (pass == 0) {
+        for (uint32_t g = tid; g < nseg; g += blockDim.x) {
+          const uint32_t c = cnt[g];
+          gbase[g] = c ? atomicAdd(fp.bcount + R.seg_base + g, c) : 0u;
+          cnt[g] = 0;
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host-side launchers (called by the engine)
 // ---------------------------------------------------------------------------
@@ -492,6 +585,12 @@ cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads
   }
   if (grid == 0) return cudaSuccess;
   sieve_segments_kernel<<<grid, threads, smem, stream>>>(prm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_fill(const FillParams& fp, uint32_t grid, cudaStream_t stream) {
+  if (grid == 0) return cudaSuccess;
+  bucket_fill_kernel<<<grid, kFillPrimes, 0, stream>>>(fp);
   return cudaGetLastError();
 }
 

@@ -37,17 +37,31 @@ struct ReqDesc {
   uint32_t tier_split;      // table index of the first mid-tier prime
   uint32_t tier_huge;       // table index of the first prime >= seg_bytes
   uint32_t rflags;          // kReqGaps: gap histogram and largest gap wanted
+  uint32_t bucket_idx;      // table index of the first bucket prime (= nprimes: none)
+  uint64_t bucket_base;     // first entry of this request's bucket lists
+  uint32_t bucket_cap;      // entries per segment list
   uint32_t pad;
 };
 
 constexpr uint32_t kReqGaps = 1u;
+constexpr uint32_t kMaxBucketSegs = 4096;    // segments of a bucket request (fill-kernel shared counts)
+constexpr uint32_t kBucketUnit = 1024;       // list entries per work unit of the sieve kernel
+constexpr uint32_t kFillPrimes = 256;        // bucket primes per fill work item
+
+// A bucket list entry: the segment-local byte (< 2^18) and the class.
+__host__ __device__ constexpr uint32_t bucket_entry(uint32_t off, uint32_t o) { return off | (o << 18); }
+
+// One fill work item: bucket primes [p0, p1) (table indices) of request req.
+struct FillItem {
+  uint32_t req, p0, p1, pad;
+};
 
 // Batch header in device memory: a captured launch reads its size from here,
 // so one CUDA graph serves every batch of a slot.
 struct BatchHdr {
   uint64_t total_segs;
   uint32_t nreq;
-  uint32_t pad;
+  uint32_t nfill;           // bucket fill items
 };
 
 // Per segment: first/last prime (absolute, 0 = none), the largest gap
@@ -101,6 +115,21 @@ struct SieveParams {
   uint32_t large_cap;
   uint32_t flags;
   uint32_t* bitmap;          // kFlagBitmap: words of request 0, from k_lo
+  const uint32_t* bucket;    // bucket list entries
+  const uint32_t* bcount;    // entries written per segment (indexed like segs)
+};
+
+struct FillParams {
+  const ReqDesc* reqs;
+  const BatchHdr* hdr;
+  const FillItem* items;
+  const uint32_t* P;
+  const uint64_t* M;
+  const uint32_t* R;
+  uint64_t rstride;
+  uint32_t* bucket;
+  uint32_t* bcount;
+  unsigned int* overflow;
 };
 
 }  // namespace vg
