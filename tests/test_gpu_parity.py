@@ -304,7 +304,8 @@ def test_bucket_lists_vs_oracle(vg, oracle_lib):
     """Primes above the bucket split marked from per-segment lists."""
     rng = random.Random(5)
     cases = [(10**14, 10**14 + 2 * 10**7), (10**14 + 10**10 - 3 * 10**7, 10**14 + 10**10 + 1),
-             (10**13 - 10**7, 10**13 + 10**7), (10**12 + 12345, 10**12 + 12345 + 4 * 10**7)]
+             (10**13 - 10**7, 10**13 + 10**7), (10**12 + 12345, 10**12 + 12345 + 4 * 10**7),
+             (10**14 - 3 * 10**9 - 7, 10**14)]
     for _ in range(6):
         a = rng.randrange(10**11, 10**14)
         cases.append((a, a + rng.randrange(7 * 10**6, 5 * 10**7)))

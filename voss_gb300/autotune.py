@@ -38,6 +38,7 @@ REGIMES = [
 SEGS = [65536, 98304, 131072, 163840, 196608, 221184]
 SPLITS = [1024, 2048, 4096, 6144, 12288]
 BUCKETS = [0, 221184, 442368, 884736, 1769472]   # bucket-list split (0 = none)
+BUCKET_MARGIN = 0.97                              # a split must beat no lists by 3%
 
 
 class TuneEntry(ctypes.Structure):
@@ -85,11 +86,13 @@ def run(quick=False, write=False, out=sys.stdout):
                 t = sum(time_range(SievePlan, stream, a, b, 3) for a, b in ranges)
                 if best is None or t < best[0]:
                     best = (t, sb, sp, 0)
-        # then the bucket split at the best segment and tier split
+        # then the bucket split at the best segment and tier split; lists
+        # must win by a clear margin (they hold device memory)
+        base_t = best[0]
         for bk in buckets[1:]:
             set_table(lib, [(U64_MAX, U64_MAX, best[1], best[2], bk)])
             t = sum(time_range(SievePlan, stream, a, b, 3) for a, b in ranges)
-            if t < best[0]:
+            if t < best[0] and t < BUCKET_MARGIN * base_t:
                 best = (t, best[1], best[2], bk)
         table.append((b_max, w_max, best[1], best[2], best[3]))
         print(f"b <= {b_max:.3g}, width <= {w_max:.3g}: seg_bytes={best[1]} tier_split={best[2]} "

@@ -46,7 +46,7 @@ def _flags() -> list[str]:
 
 def _newest_input() -> float:
     files = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + \
-        list((ROOT / "include" / "voss").glob("*.h")) + [Path(__file__)]
+        list(CSRC.glob("*.inc")) + list((ROOT / "include" / "voss").glob("*.h")) + [Path(__file__)]
     return max(f.stat().st_mtime for f in files)
 
 

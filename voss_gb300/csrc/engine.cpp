@@ -286,6 +286,10 @@ uint64_t Plan::bucket_bytes_for(uint64_t a, uint64_t b) const {
   return bp.cap ? 4ull * bp.cap * nseg : 0;
 }
 
+uint32_t Plan::fill_grid_max() const {
+  return eng->sm_count * bucket_fill_ctas_per_sm();
+}
+
 bool Plan::overflowed() const {
   return nfill && host_flag.ptr && *static_cast<const unsigned int*>(host_flag.ptr) != 0;
 }
@@ -357,15 +361,34 @@ void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
       const Config c = E.tuned_for(r.a, r.b, many);
       const BucketPlan bp = E.bucket_plan(c, r.b, r.nprimes, r.nseg, r.seg_bytes);
       const uint64_t need = (uint64_t)bp.cap * r.nseg;
-      const uint64_t items_need = (r.nprimes - bp.bucket_idx + kFillPrimes - 1) / kFillPrimes;
-      const bool fits = !cap_req || (bbase + need <= cap_bucket && host_fills.size() + items_need <= cap_fill);
-      if (bp.cap && fits) {
-        r.bucket_idx = bp.bucket_idx;
-        r.bucket_cap = bp.cap;
-        r.bucket_base = bbase;
-        bbase += need;
-        for (uint32_t p0 = bp.bucket_idx; p0 < r.nprimes; p0 += kFillPrimes)
-          host_fills.push_back(FillItem{i, p0, std::min<uint32_t>(p0 + kFillPrimes, r.nprimes), 0});
+      if (bp.cap) {
+        // fill items: runs of kFillPrimes primes; a run's hits (8 per p
+        // bytes per prime) split over segment ranges so that every item
+        // carries at most about kFillHits hits: items balance, and the list
+        // blocks that the resident fill CTAs are writing at any time (their
+        // items' entries) stay well inside L2, so lines leave it complete
+        const uint32_t nseg = (uint32_t)r.nseg;
+        const double per = 8.0 * (double)(r.k_hi - r.k_lo);
+        const double target = kFillHits;
+        item_buf.clear();
+        for (uint32_t p0 = bp.bucket_idx; p0 < r.nprimes; p0 += kFillPrimes) {
+          const uint32_t p1 = std::min<uint32_t>(p0 + kFillPrimes, r.nprimes);
+          const double hits = per * (E.hInvPrefix[p1] - E.hInvPrefix[p0]);
+          const uint32_t pieces = (uint32_t)std::min<double>(nseg, std::max(1.0, std::ceil(hits / target)));
+          for (uint32_t j = 0; j < pieces; ++j) {
+            const uint32_t g0 = (uint32_t)((uint64_t)nseg * j / pieces);
+            const uint32_t g1 = (uint32_t)((uint64_t)nseg * (j + 1) / pieces);
+            item_buf.push_back(FillItem{i, p0, p1, g0 | (g1 << 16)});
+          }
+        }
+        const bool fits = !cap_req || (bbase + need <= cap_bucket && host_fills.size() + item_buf.size() <= cap_fill);
+        if (fits) {
+          r.bucket_idx = bp.bucket_idx;
+          r.bucket_cap = bp.cap;
+          r.bucket_base = bbase;
+          bbase += need;
+          host_fills.insert(host_fills.end(), item_buf.begin(), item_buf.end());
+        }
       }
     }
   }
@@ -509,8 +532,7 @@ void Plan::run_device(cudaStream_t s) {
     fp.bucket = bucket.as<uint32_t>();
     fp.bcount = bcount.as<uint32_t>();
     fp.overflow = overflow.as<unsigned int>();
-    const uint32_t fgrid = cap_req ? eng->sm_count * 4
-                                   : (uint32_t)std::min<uint64_t>(nfill, (uint64_t)eng->sm_count * 4);
+    const uint32_t fgrid = cap_req ? fill_grid_max() : std::min<uint32_t>(nfill, fill_grid_max());
     check_cuda(launch_bucket_fill(fp, fgrid, s), "bucket_fill_kernel");
   }
   check_cuda(launch_sieve(prm, grid, threads, s), "sieve_segments_kernel");

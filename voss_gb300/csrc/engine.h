@@ -92,6 +92,7 @@ struct Plan {
   uint32_t cap_fill = 0;
   bool allow_buckets = true;
   std::vector<FillItem> host_fills;
+  std::vector<FillItem> item_buf;   // one request's fill items, before the capacity check
   HostPinned stage;             // BatchHdr followed by ReqDesc[cap]
   HostPinned host_results;      // ReqResult[] in device order
   HostPinned host_flag;         // the overflow flag, copied with the results
@@ -144,6 +145,8 @@ struct Plan {
   // True if the last run's bucket lists overflowed (its results are then
   // invalid); valid once the stream has passed fetch_async().
   bool overflowed() const;
+  // resident CTAs of the bucket fill kernel over the whole GPU
+  uint32_t fill_grid_max() const;
 };
 
 // Bucket layout of one request: first bucket prime, list capacity per
@@ -218,6 +221,7 @@ size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads);
 cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads,
                          cudaStream_t stream);
 cudaError_t launch_bucket_fill(const FillParams& fp, uint32_t grid, cudaStream_t stream);
+uint32_t bucket_fill_ctas_per_sm();      // resident fill CTAs per SM (occupancy query, cached)
 cudaError_t launch_finalize(const ReqDesc* reqs, const BatchHdr* hdr, const SegRec* segs,
                             ReqAccum* acc, LargeGapRec* large, unsigned int* n_large,
                             uint32_t large_cap, ReqResult* out, uint32_t grid,

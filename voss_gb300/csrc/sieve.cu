@@ -493,62 +493,98 @@ finalize_kernel(const ReqDesc* __restrict__ reqs, const BatchHdr* __restrict__ h
   }
 }
 
-// Bucket fill: one CTA per work item (a request and a run of its bucket
-// primes).  Pass 1 counts the hits of every prime (thread per prime, all eight
-// classes) per segment in shared memory; one global atomic per segment then
-// reserves room in that segment's list; pass 2 recomputes the hits and writes
-// the entries.  A list that would overflow its capacity raises *overflow and
-// drops the entry (the host then reruns without buckets).
+// Bucket fill: one CTA per work item (a request, a run of its bucket primes
+// and a run of its segments; heavy runs of small primes are split over
+// several items so that items carry similar numbers of hits), a thread per
+// prime walking its eight classes.  Pass 1 counts the hits per segment in
+// shared memory; one global atomic per segment reserves room in that
+// segment's list and leaves the reserved base in the shared counter; pass 2
+// walks the hits again and writes each entry at the counter's next slot.  A
+// hit's segment and offset advance by p = pq*S + pr without a division.  A
+// list that would overflow its capacity raises *overflow and drops the entry
+// (the host then reruns without lists).
 __global__ void __launch_bounds__(kFillPrimes)
 bucket_fill_kernel(const FillParams fp) {
   __shared__ uint32_t cnt[kMaxBucketSegs];
-  __shared__ uint32_t gbase[kMaxBucketSegs];
   const uint32_t tid = threadIdx.x;
   const uint32_t nitems = fp.hdr->nfill;
   for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
     const FillItem item = fp.items[it];
     const ReqDesc R = fp.reqs[item.req];
-    const uint32_t nseg = (uint32_t)R.nseg;
+    const uint32_t g0 = item.segs & 0xFFFFu, g1 = item.segs >> 16;
+    const uint32_t nseg = g1 - g0;
     const uint32_t S = R.seg_bytes;
     const uint64_t k0 = R.k_lo;
     const uint32_t total = (uint32_t)(R.k_hi - R.k_lo);
+    const uint32_t lo = g0 * S;
+    const uint32_t hi = min(total, g1 * S);
+    const uint32_t cap = R.bucket_cap;
+    uint32_t* const list = fp.bucket + R.bucket_base + (uint64_t)g0 * cap;
+    unsigned int* const gcount = fp.bcount + R.seg_base + g0;
     const float inv_s = 1.0f / (float)S;
-    for (uint32_t i = tid; i < nseg; i += blockDim.x) cnt[i] = 0;
+    // q = x / S, r = x % S for x < 2^30: a float estimate, corrected once
+    auto divmod_s = [&](uint32_t x, uint32_t& r) {
+      uint32_t q = __float2uint_rz((float)x * inv_s);
+      int32_t d = (int32_t)(x - q * S);
+      if (d < 0) { --q; d += (int32_t)S; } else if (d >= (int32_t)S) { ++q; d -= (int32_t)S; }
+      r = (uint32_t)d;
+      return q;
+    };
+    for (uint32_t g = tid; g < nseg; g += blockDim.x) cnt[g] = 0;
     __syncthreads();
     const uint32_t i = item.p0 + tid;
     const bool valid = i < item.p1;
-    uint32_t p = 0, m = 0;
+    uint32_t p = 0, m = 0, pq = 0, pr = 0;
     bool low = false;
     if (valid) {
       p = __ldg(fp.P + i);
       m = mod_barrett(k0, p, __ldg(fp.M + i));
       low = 30ull * k0 < (uint64_t)p * p;
+      pq = divmod_s(p, pr);
     }
-    // segment of byte k: float estimate of k / S, corrected by one step
-    auto seg_of = [&](uint32_t k, uint32_t& off) {
-      uint32_t q = __float2uint_rz((float)k * inv_s);
-      int64_t r = (int64_t)k - (int64_t)q * S;
-      if (r < 0) { --q; r += S; } else if (r >= S) { ++q; r -= S; }
-      off = (uint32_t)r;
-      return q;
-    };
-    for (int pass = 0; pass < 2; ++pass) {
+    // first hit at or after segment g0 of each class, kept for both passes
+    // (hi = none); the eight residue loads issue together
+    uint32_t first[8];
+#pragma unroll
+    for (int o = 0; o < 8; ++o) first[o] = valid ? __ldg(fp.R + o * fp.rstride + i) : 0u;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      uint32_t k = hi;
       if (valid) {
-#pragma unroll 1
-        for (uint32_t o = 0; o < 8; ++o) {
-          const uint32_t r = __ldg(fp.R + o * fp.rstride + i);
-          uint32_t s = r >= m ? r - m : r + p - m;
-          if (low) s = lift_to_square(s, k0, p, o, total);
-          for (uint32_t k = s; k < total; k += p) {
-            uint32_t off;
-            const uint32_t sg = seg_of(k, off);
-            if (pass == 0) {
-              atomicAdd(&cnt[sg], 1u);
-            } else {
-              const uint32_t pos = gbase[sg] + atomicAdd(&cnt[sg], 1u);
-              if (pos < R.bucket_cap) fp.bucket[R.bucket_base + (uint64_t)sg * R.bucket_cap + pos] = bucket_entry(off, o);
-              else atomicOr(fp.overflow, 1u);
-            }
+        const uint32_t r = first[o];
+        k = r >= m ? r - m : r + p - m;
+        if (low) k = lift_to_square(k, k0, p, o, total);
+        if (k < lo) k += ((lo - k + p - 1) / p) * p;
+        k = min(k, hi);
+      }
+      first[o] = k;
+    }
+    // (Lanes of a warp hold primes of nearly the same size and walk in
+    // step, so many of them meet on one segment counter at a time; the
+    // counter then hands them consecutive slots and their entries leave in
+    // shared sectors.  Spreading the lanes over segments removes the atomic
+    // conflicts but scatters the stores, and measured slower.)
+    for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll
+      for (int o = 0; o < 8; ++o) {
+        uint32_t k = first[o];
+        if (k >= hi) continue;
+        uint32_t off;
+        uint32_t sg = divmod_s(k, off) - g0;                // segment, relative to g0
+        if (pass == 0) {
+          for (; k < hi; k += p) {
+            atomicAdd(&cnt[sg], 1u);
+            off += pr; sg += pq;
+            if (off >= S) { off -= S; ++sg; }
+          }
+        } else {
+          const uint32_t tag = (uint32_t)o << 18;
+          for (; k < hi; k += p) {
+            const uint32_t pos = atomicAdd(&cnt[sg], 1u);
+            if (pos < cap) list[(size_t)sg * cap + pos] = tag | off;
+            else atomicOr(fp.overflow, 1u);
+            off += pr; sg += pq;
+            if (off >= S) { off -= S; ++sg; }
           }
         }
       }
@@ -556,8 +592,7 @@ bucket_fill_kernel(const FillParams fp) {
       if (pass == 0) {
         for (uint32_t g = tid; g < nseg; g += blockDim.x) {
           const uint32_t c = cnt[g];
-          gbase[g] = c ? atomicAdd(fp.bcount + R.seg_base + g, c) : 0u;
-          cnt[g] = 0;
+          cnt[g] = c ? atomicAdd(gcount + g, c) : 0u;
         }
         __syncthreads();
       }
@@ -586,6 +621,13 @@ cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads
   if (grid == 0) return cudaSuccess;
   sieve_segments_kernel<<<grid, threads, smem, stream>>>(prm);
   return cudaGetLastError();
+}
+
+uint32_t bucket_fill_ctas_per_sm() {
+  static int n = 0;
+  if (!n && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bucket_fill_kernel, kFillPrimes, 0) != cudaSuccess || n < 1))
+    n = 1;
+  return (uint32_t)n;
 }
 
 cudaError_t launch_bucket_fill(const FillParams& fp, uint32_t grid, cudaStream_t stream) {

@@ -44,16 +44,18 @@ struct ReqDesc {
 };
 
 constexpr uint32_t kReqGaps = 1u;
-constexpr uint32_t kMaxBucketSegs = 4096;    // segments of a bucket request (fill-kernel shared counts)
+constexpr uint32_t kMaxBucketSegs = 4096;    // segments of a bucket request (fill-kernel shared counts, 16-bit packing)
 constexpr uint32_t kBucketUnit = 1024;       // list entries per work unit of the sieve kernel
 constexpr uint32_t kFillPrimes = 256;        // bucket primes per fill work item
+constexpr uint32_t kFillHits = 16384;        // list entries per fill work item, about
 
 // A bucket list entry: the segment-local byte (< 2^18) and the class.
 __host__ __device__ constexpr uint32_t bucket_entry(uint32_t off, uint32_t o) { return off | (o << 18); }
 
-// One fill work item: bucket primes [p0, p1) (table indices) of request req.
+// One fill work item: the hits of bucket primes [p0, p1) (table indices) of
+// request req that fall in its segments [g0, g1), packed g0 | g1 << 16.
 struct FillItem {
-  uint32_t req, p0, p1, pad;
+  uint32_t req, p0, p1, segs;
 };
 
 // Batch header in device memory: a captured launch reads its size from here,
