@@ -243,8 +243,14 @@ def serving(torch, n=2000):
         srv.reset_metrics()
         res2, lat2, wall2 = run_served(srv, reqs, rate=rate, seed=3)
         m_rate = srv.metrics()
+    # the same server with each request sieved on its own (no shared pieces):
+    # what continuous batching alone gives
+    with Server(share=False) as srv:
+        run_served(srv, warm)
+        res3, lat3, wall3 = run_served(srv, reqs)
     ok = all(same_answer(r, x, y) for r, x, y in zip(reqs, res, plain)) and \
-        all(same_answer(r, x, y) for r, x, y in zip(reqs, res2, plain))
+        all(same_answer(r, x, y) for r, x, y in zip(reqs, res2, plain)) and \
+        all(same_answer(r, x, y) for r, x, y in zip(reqs, res3, plain))
     ints = sum(r.b - r.a for r in reqs)
     lat_s, lat_r = sorted(lat), sorted(lat2)
     q = lambda v, f: v[min(len(v) - 1, int(f * (len(v) - 1) + 0.5))]
@@ -252,6 +258,7 @@ def serving(torch, n=2000):
             "plain_req_per_s": n / plain_s, "plain_s": plain_s,
             "served_req_per_s": n / wall, "served_s": wall,
             "speedup_req_per_s": plain_s / wall,
+            "isolated_req_per_s": n / wall3, "isolated_speedup_req_per_s": plain_s / wall3,
             "served_p50_ms": q(lat_s, 0.5) / 1e3, "served_p99_ms": q(lat_s, 0.99) / 1e3,
             "batches": m_sat["batches"], "mean_batch": m_sat["mean_batch"],
             "max_inflight_batches": m_sat["max_inflight_batches"],

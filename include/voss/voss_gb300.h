@@ -52,7 +52,11 @@ int voss_primes_range_stats_ex(uint64_t a, uint64_t b, voss_range_stats_t* out,
                                uint64_t* hist_full);
 
 /* n independent ranges in one launch (one persistent kernel over all their
- * segments).  out[i] is the result of [a[i], b[i]). */
+ * segments).  out[i] is the result of [a[i], b[i]).  Ranges that overlap
+ * sieve their common integers once: the ranges are cut at every endpoint
+ * into disjoint pieces, each piece is sieved once and each range is rebuilt
+ * from its pieces, gaps stitched where they meet; results are the same as
+ * one call per range. */
 int voss_primes_range_stats_batch(uint64_t n, const uint64_t* a, const uint64_t* b,
                                   voss_range_stats_t* out);
 
@@ -184,6 +188,10 @@ typedef struct {
     uint64_t memory_budget;       /* device bytes over all batches in flight */
     uint32_t use_graphs;          /* replay a captured CUDA graph per batch */
     uint64_t bucket_bytes;        /* bucket-list arena per slot (default 256 MiB) */
+    uint32_t isolate_requests;    /* nonzero: each request of a batch is sieved on
+                                     its own; default (0): overlapping requests of
+                                     a batch share the sieving of their common
+                                     integers (results are the same either way) */
 } voss_gb300_server_config_t;
 
 typedef struct {

@@ -336,3 +336,29 @@ def test_bucket_overflow_falls_back(vg, oracle_lib):
             assert got.count == want["count"] and got.max_gap == want["max_gap"]
     finally:
         vg.primes.set_config(**base)
+
+
+PUBLIC_KEYS = ("count", "twins", "cousins", "sexy", "pi_4_1", "pi_4_3", "pi_3_1", "pi_3_2", "first_prime",
+               "last_prime", "max_gap", "max_gap_start", "num_gaps", "large_gaps", "gap_hist")
+
+
+def test_batch_shares_overlapping_ranges(vg):
+    """Overlapping, nested, duplicated and touching ranges in one batch: each
+    is rebuilt from shared pieces and must equal its own call."""
+    g0 = 738832927927            # the gap of 540 below 10^12: pieces cut inside it
+    ranges = [(0, 10), (2, 3), (3, 4), (0, 3), (5, 100), (0, 1000), (7, 8), (5, 5), (0, 2), (1, 2),
+              (10**9, 10**9 + 10**7), (10**9 + 1234, 10**9 + 5 * 10**6), (10**9 + 5 * 10**6, 10**9 + 2 * 10**7),
+              (10**9, 10**9 + 10**7), (10**9 + 10**7 - 1, 10**9 + 10**7 + 1),
+              (g0 - 1000, g0 + 1000), (g0 + 100, g0 + 3000), (g0 + 540, g0 + 541), (g0 - 10**6, g0 + 10**6),
+              (10**12, 10**12 + 10**9), (10**12 + 3 * 10**8, 10**12 + 3 * 10**8 + 1),
+              (10**12 + 10**8, 10**12 + 2 * 10**9), (0, 10**8), (10**7, 3 * 10**7)]
+    rng = random.Random(11)
+    for _ in range(40):
+        a = rng.choice([0, 10**6, 10**9, 10**11]) + rng.randrange(0, 10**8)
+        ranges.append((a, a + rng.randrange(0, 10**8)))
+    got = vg.range_stats_batch(ranges)
+    for (a, b), g in zip(ranges, got):
+        alone = vg.range_stats(a, b)
+        for k in PUBLIC_KEYS:
+            assert getattr(g, k) == getattr(alone, k), (a, b, k, getattr(g, k), getattr(alone, k))
+    assert got[15].max_gap == 540 and got[18].max_gap == 540

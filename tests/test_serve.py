@@ -70,3 +70,18 @@ def test_server_rejects_oversized_and_bad_ops(vg):
         assert got.count == 168
         with pytest.raises(vg.VossError):
             srv.result(t)                          # already collected
+
+
+@pytest.mark.gpu
+def test_shared_and_isolated_servers_agree(vg):
+    """The default server shares the sieving of overlapping requests; a
+    server with isolated requests must give the same answers."""
+    from voss_gb300.serve import Server, run_served, same_answer, serving_mix
+    reqs = serving_mix(600, seed=3, max_start=1e11)
+    reqs = [r for r in reqs if r.b - r.a <= 3 * 10**8]
+    with Server(slots=2, max_batch=128) as srv:
+        shared, _, _ = run_served(srv, reqs)
+    with Server(slots=2, max_batch=128, share=False) as srv:
+        alone, _, _ = run_served(srv, reqs)
+    for r, x, y in zip(reqs, shared, alone):
+        assert same_answer(r, x, y), (r, x, y)

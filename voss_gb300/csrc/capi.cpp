@@ -624,7 +624,7 @@ extern "C" int voss_primes_range_stats_batch(uint64_t n, const uint64_t* a, cons
   return guarded([&] {
     vg::Engine& E = vg::Engine::for_current_device();
     std::lock_guard<std::mutex> g(E.mu);
-    const vg::ReqResult* r = E.run((uint32_t)n, a, b);
+    const vg::ReqResult* r = E.run((uint32_t)n, a, b, nullptr, true, true);
     for (uint64_t i = 0; i < n; ++i) vg::to_public(r[i], a[i], b[i], out + i);
     return VOSS_OK;
   }, VOSS_ERR_INTERNAL);
@@ -886,6 +886,7 @@ extern "C" int voss_gb300_server_create(const voss_gb300_server_config_t* c, vos
       if (c->memory_budget) sc.mem_budget = c->memory_budget;
       if (c->bucket_bytes) sc.bucket_bytes = c->bucket_bytes;
       sc.use_graphs = c->use_graphs;
+      sc.share = c->isolate_requests ? 0u : 1u;
     }
     vg::Engine& E = vg::Engine::for_current_device();
     auto* h = new voss_gb300_server();

@@ -263,6 +263,14 @@ BucketPlan Engine::bucket_plan(const Config& c, uint64_t b, uint32_t nprimes, ui
 void Plan::reserve_capacity(uint32_t max_req, uint64_t max_segs, uint64_t max_bucket_entries) {
   cap_req = std::max<uint32_t>(max_req, 1);
   cap_segs = std::max<uint64_t>(max_segs, 1);
+  if (share) {
+    cap_out = cap_req;
+    cap_req = 2 * cap_out;
+    cap_segs += 4ull * cap_out;
+    spans.reserve(sizeof(ReqSpan) * cap_out);
+    apos.reserve(sizeof(uint32_t) * cap_req);
+    rres.reserve(sizeof(ReqResult) * cap_out);
+  }
   cap_bucket = max_bucket_entries;
   cap_fill = max_bucket_entries ? 65536u : 0u;
   if (cap_bucket) bucket.reserve(4 * cap_bucket);
@@ -303,6 +311,75 @@ uint64_t Plan::segments_for(uint64_t a, uint64_t b) const {
 
 void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
                 const uint32_t* rflags) {
+  nout = 0;
+  if (!share || (fl & kFlagBitmap)) {
+    load_requests(n, a, b, fl, rflags);
+    return;
+  }
+  if (cap_out && n > cap_out) throw Error(VOSS_ERR_INVALID_ARG, "batch exceeds the plan's capacity");
+  // Cut the ranges at every endpoint; keep the pieces some request covers.
+  std::vector<uint64_t> pts;
+  pts.reserve(2 * n);
+  for (uint32_t i = 0; i < n; ++i)
+    if (b[i] > a[i]) { pts.push_back(a[i]); pts.push_back(b[i]); }
+  std::sort(pts.begin(), pts.end());
+  pts.erase(std::unique(pts.begin(), pts.end()), pts.end());
+  const size_t np = pts.size();
+  std::vector<int32_t> cov(np + 1, 0), gcov(np + 1, 0);
+  auto at = [&](uint64_t x) { return (size_t)(std::lower_bound(pts.begin(), pts.end(), x) - pts.begin()); };
+  for (uint32_t i = 0; i < n; ++i) {
+    if (b[i] <= a[i]) continue;
+    const size_t ia = at(a[i]), ib = at(b[i]);
+    ++cov[ia]; --cov[ib];
+    if (!rflags || (rflags[i] & kReqGaps)) { ++gcov[ia]; --gcov[ib]; }
+  }
+  atom_a.clear(); atom_b.clear(); atom_rf.clear();
+  std::vector<uint32_t> atom_of(np, UINT32_MAX);      // elementary piece k -> atom
+  int32_t c = 0, g = 0;
+  for (size_t k = 0; k + 1 < np; ++k) {
+    c += cov[k];
+    g += gcov[k];
+    if (c > 0) {
+      atom_of[k] = (uint32_t)atom_a.size();
+      atom_a.push_back(pts[k]);
+      atom_b.push_back(pts[k + 1]);
+      atom_rf.push_back(g > 0 ? kReqGaps : 0u);
+    }
+  }
+  // A fixed-capacity plan takes the atoms only if they fit (narrow atoms may
+  // be tuned to smaller segments than the requests they came from);
+  // otherwise the batch runs unshared, which always fits.
+  if (cap_out) {
+    uint64_t segs_need = 0;
+    for (size_t i = 0; i < atom_a.size(); ++i) segs_need += segments_for(atom_a[i], atom_b[i]);
+    if (atom_a.size() > cap_req || segs_need > cap_segs) {
+      load_requests(n, a, b, fl, rflags);
+      return;
+    }
+  }
+  host_spans.assign(n, ReqSpan{0, 0, 0, 0});
+  for (uint32_t i = 0; i < n; ++i) {
+    host_spans[i].rflags = rflags ? rflags[i] : kReqGaps;
+    if (b[i] <= a[i]) continue;
+    // every piece inside the request is covered, so its atoms are contiguous
+    host_spans[i].s = atom_of[at(a[i])];
+    host_spans[i].e = atom_of[at(b[i]) - 1] + 1;
+  }
+  load_requests((uint32_t)atom_a.size(), atom_a.data(), atom_b.data(), fl, atom_rf.data());
+  host_apos.assign(nreq, 0);
+  for (uint32_t d = 0; d < nreq; ++d) host_apos[order[d]] = d;   // position -> device index
+  nout = n;
+  static_cast<BatchHdr*>(stage.ptr)->nout = nout;
+  if (!cap_out) {
+    spans.reserve(sizeof(ReqSpan) * std::max<uint32_t>(n, 1));
+    apos.reserve(sizeof(uint32_t) * std::max<uint32_t>(nreq, 1));
+    rres.reserve(sizeof(ReqResult) * std::max<uint32_t>(n, 1));
+    host_results.reserve(sizeof(ReqResult) * std::max<uint32_t>(std::max(n, nreq), 1));
+  }
+}
+
+void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
+                         const uint32_t* rflags) {
   Engine& E = *eng;
   flags = fl;
   uint64_t max_b = 0;
@@ -427,6 +504,8 @@ void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
   h->total_segs = total_segs;
   h->nreq = nreq;
   h->nfill = nfill;
+  h->nout = 0;
+  h->pad = 0;
   if (n) std::memcpy(h + 1, host_reqs.data(), sizeof(ReqDesc) * n);
   const uint64_t gcap = (uint64_t)E.sm_count * E.cfg.ctas_per_sm;
   grid = (uint32_t)(cap_req ? gcap : std::min<uint64_t>(total_segs, gcap));
@@ -467,6 +546,13 @@ void Plan::upload(cudaStream_t s) {
   if (nfill)
     check_cuda(cudaMemcpyAsync(fills.ptr, host_fills.data(), sizeof(FillItem) * nfill,
                                cudaMemcpyHostToDevice, s), "upload fill items");
+  if (nout) {
+    check_cuda(cudaMemcpyAsync(spans.ptr, host_spans.data(), sizeof(ReqSpan) * nout,
+                               cudaMemcpyHostToDevice, s), "upload request spans");
+    if (nreq)
+      check_cuda(cudaMemcpyAsync(apos.ptr, host_apos.data(), sizeof(uint32_t) * nreq,
+                                 cudaMemcpyHostToDevice, s), "upload atom order");
+  }
 }
 
 Plan::~Plan() {
@@ -541,11 +627,18 @@ void Plan::run_device(cudaStream_t s) {
                              acc.as<ReqAccum>(), large.as<LargeGapRec>(),
                              nlarge.as<unsigned int>(), large_cap, results.as<ReqResult>(), nacc, s),
              "finalize_kernel");
+  if (cap_req ? cap_out : nout)
+    check_cuda(launch_combine(hdr.as<BatchHdr>(), spans.as<ReqSpan>(), apos.as<uint32_t>(),
+                              results.as<ReqResult>(), rres.as<ReqResult>(), cap_req ? cap_out : nout, s),
+               "combine_kernel");
   check_cuda(cudaEventRecord(ev[2], s), "event");
 }
 
 void Plan::fetch_async(cudaStream_t s) {
-  if (nreq)
+  if (nout)
+    check_cuda(cudaMemcpyAsync(host_results.ptr, rres.ptr, sizeof(ReqResult) * nout,
+                               cudaMemcpyDeviceToHost, s), "download results");
+  else if (nreq)
     check_cuda(cudaMemcpyAsync(host_results.ptr, results.ptr, sizeof(ReqResult) * nreq,
                                cudaMemcpyDeviceToHost, s), "download results");
   if (nfill) {
@@ -556,8 +649,12 @@ void Plan::fetch_async(cudaStream_t s) {
 }
 
 const ReqResult* Plan::finish() {
-  out.resize(nreq);
   const ReqResult* r = static_cast<const ReqResult*>(host_results.ptr);
+  if (nout) {                          // combine_kernel wrote caller order
+    out.assign(r, r + nout);
+    return out.data();
+  }
+  out.resize(nreq);
   for (uint32_t i = 0; i < nreq; ++i) out[order[i]] = r[i];
   return out.data();
 }
@@ -614,8 +711,10 @@ uint64_t Plan::algorithmic_clears() const {
 }
 
 const ReqResult* Engine::run(uint32_t n, const uint64_t* a, const uint64_t* b,
-                             std::vector<LargeGapRec>* lg, bool gaps) {
+                             std::vector<LargeGapRec>* lg, bool gaps, bool share) {
   std::vector<uint32_t> rf(n, gaps ? kReqGaps : 0u);
+  struct Unshare { Plan& p; ~Unshare() { p.share = false; } } unshare{scratch};
+  scratch.share = share && !lg && n > 1;
   scratch.allow_buckets = true;
   scratch.load(n, a, b, 0, rf.data());
   scratch.launch(stream);

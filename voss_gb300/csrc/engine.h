@@ -91,10 +91,21 @@ struct Plan {
   uint32_t nfill = 0;
   uint32_t cap_fill = 0;
   bool allow_buckets = true;
+  // Shared atoms: a batch's ranges are cut at every endpoint into disjoint
+  // atoms, each sieved once (with gap outputs if any request over it wants
+  // them); combine_kernel then rebuilds each caller request from its atoms.
+  bool share = false;
+  uint32_t nout = 0;            // caller requests of a shared batch (0: not shared)
+  uint32_t cap_out = 0;         // fixed capacity of caller requests (shared plans)
+  DevBuf spans, apos, rres;     // ReqSpan per caller, atom device index by position, caller results
+  std::vector<ReqSpan> host_spans;
+  std::vector<uint32_t> host_apos;
+  std::vector<uint64_t> atom_a, atom_b;
+  std::vector<uint32_t> atom_rf;
   std::vector<FillItem> host_fills;
   std::vector<FillItem> item_buf;   // one request's fill items, before the capacity check
   HostPinned stage;             // BatchHdr followed by ReqDesc[cap]
-  HostPinned host_results;      // ReqResult[] in device order
+  HostPinned host_results;      // ReqResult[] in device order (caller order when shared)
   HostPinned host_flag;         // the overflow flag, copied with the results
   std::vector<ReqResult> out;   // caller order
   uint32_t large_cap = 1u << 16;
@@ -111,11 +122,16 @@ struct Plan {
   static constexpr uint32_t kKernels = 2;
 
   // Fix the capacity (requests, segments, bucket entries) of a
-  // graph-replayed plan.
+  // graph-replayed plan.  With share set, max_req and max_segs are the
+  // caller's limits; the atoms get room for at most 2*max_req - 1 pieces,
+  // each adding at most two partial segments.
   void reserve_capacity(uint32_t max_req, uint64_t max_segs, uint64_t max_bucket_entries = 0);
   // rflags: per request kReqGaps (NULL = all requests want gaps)
   void load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t flags,
             const uint32_t* rflags = nullptr);
+  // The device requests themselves (load() passes atoms here when sharing).
+  void load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t flags,
+                     const uint32_t* rflags);
   void upload(cudaStream_t s);
   void run_device(cudaStream_t s);
   void prepare(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t flags);
@@ -202,9 +218,11 @@ class Engine {
                          uint32_t seg_bytes) const;
   std::vector<TuneEntry> tuning;
 
-  // Run ranges synchronously on the engine stream.
+  // Run ranges synchronously on the engine stream.  share: overlapping
+  // ranges sieve their common integers once (not with large-gap output).
   const ReqResult* run(uint32_t n, const uint64_t* a, const uint64_t* b,
-                       std::vector<LargeGapRec>* large = nullptr, bool gaps = true);
+                       std::vector<LargeGapRec>* large = nullptr, bool gaps = true,
+                       bool share = false);
 
  private:
   Engine() = default;
@@ -222,6 +240,8 @@ cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads
                          cudaStream_t stream);
 cudaError_t launch_bucket_fill(const FillParams& fp, uint32_t grid, cudaStream_t stream);
 uint32_t bucket_fill_ctas_per_sm();      // resident fill CTAs per SM (occupancy query, cached)
+cudaError_t launch_combine(const BatchHdr* hdr, const ReqSpan* spans, const uint32_t* apos,
+                           const ReqResult* ares, ReqResult* out, uint32_t grid, cudaStream_t stream);
 cudaError_t launch_finalize(const ReqDesc* reqs, const BatchHdr* hdr, const SegRec* segs,
                             ReqAccum* acc, LargeGapRec* large, unsigned int* n_large,
                             uint32_t large_cap, ReqResult* out, uint32_t grid,

@@ -172,6 +172,7 @@ __global__ void na_init_kernel(NaScratch* s, ReqDesc r) {
     s->hdr.total_segs = r.nseg;
     s->hdr.nreq = 1;
     s->hdr.nfill = 0;
+    s->hdr.nout = 0;
     s->queue = 0;
     s->nlarge = 0;
     s->req = r;

@@ -14,7 +14,12 @@
 //   * batches in different slots overlap on the device: CTAs of the next
 //     batch start as SMs free up from the previous one;
 //   * the sieving-prime table and tiles stay resident; count and Chebyshev
-//     requests skip the ordered gap scan.
+//     requests skip the ordered gap scan;
+//   * requests of one batch share work: their ranges are cut at every
+//     endpoint into disjoint atoms, each atom is sieved once, and a combine
+//     kernel rebuilds every request from its run of atoms (gaps stitched
+//     where atoms meet), so overlapping requests do not sieve the same
+//     integers twice.
 // A result is the same whether the request ran alone or in a batch.
 #include "serve.h"
 
@@ -50,6 +55,7 @@ Server::Server(Engine& e, const ServerConfig& c) : E(e), cfg(c) {
     s.plan.eng = &E;
     s.plan.device = E.device;
     s.plan.batch_mode = true;
+    s.plan.share = cfg.share != 0;
     s.plan.reserve_capacity(cfg.max_batch, cfg.max_segs, cfg.bucket_bytes / 4);
     check_cuda(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "server stream");
     check_cuda(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "server event");

@@ -26,6 +26,7 @@ struct ServerConfig {
   uint64_t mem_budget = 1ull << 30;   // device bytes over all batches in flight
   uint32_t use_graphs = 1;
   uint64_t bucket_bytes = 256ull << 20;   // bucket-list arena per slot
+  uint32_t share = 1;            // batches sieve shared atoms of their ranges once
 };
 
 class Server {

@@ -600,6 +600,89 @@ bucket_fill_kernel(const FillParams fp) {
   }
 }
 
+// Rebuild caller requests from shared atoms (disjoint pieces of the batch's
+// ranges, each sieved once).  A request is the ordered run of its atoms:
+// counts add; its gaps are the atoms' inner gaps plus one junction gap
+// between each atom holding primes and the next such atom; the maximal gap
+// is the largest of those, the earliest on ties, as within one range.  Each
+// thread folds a contiguous run of atoms, thread 0 joins the runs in order.
+// A request that asked for counts only gets no gap outputs even where its
+// atoms were scanned for another request's gaps, so its result is the one
+// it gets alone.
+__global__ void __launch_bounds__(256)
+combine_kernel(const BatchHdr* __restrict__ hdr, const ReqSpan* __restrict__ spans,
+               const uint32_t* __restrict__ apos, const ReqResult* __restrict__ ares,
+               ReqResult* __restrict__ out) {
+  const uint32_t r = blockIdx.x, tid = threadIdx.x;
+  if (r >= hdr->nout) return;
+  const ReqSpan sp = spans[r];
+  const bool gaps = (sp.rflags & kReqGaps) != 0;
+  __shared__ uint32_t jh[kHistBins];
+  __shared__ uint64_t t_first[256], t_last[256], t_bg[256], t_bs[256];
+  __shared__ uint64_t t_sum[5][256];
+  for (uint32_t b = tid; b < (uint32_t)kHistBins; b += blockDim.x) jh[b] = 0;
+  __syncthreads();
+
+  auto add_gap = [&](uint64_t g, uint64_t st, uint64_t& bg, uint64_t& bs) {
+    const uint64_t bin = g >> 1;
+    atomicAdd(&jh[bin < (uint64_t)kHistBins ? bin : kHistBins - 1], 1u);
+    if (g > bg || (g == bg && st < bs)) { bg = g; bs = st; }
+  };
+  const uint32_t n = sp.e - sp.s;
+  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+  const uint32_t j0 = sp.s + min(n, tid * per), j1 = sp.s + min(n, (tid + 1) * per);
+  uint64_t c[5] = {0, 0, 0, 0, 0};
+  uint64_t first = 0, last = 0, bg = 0, bs = 0;
+  for (uint32_t j = j0; j < j1; ++j) {
+    const ReqResult* A = ares + apos[j];
+    const uint64_t ac = A->count;
+    c[0] += ac; c[1] += A->c41; c[2] += A->c43; c[3] += A->c31; c[4] += A->c32;
+    if (!ac) continue;
+    if (!first) first = A->first;
+    if (gaps) {
+      if (last) add_gap(A->first - last, last, bg, bs);
+      const uint64_t mg = A->max_gap;
+      if (mg && (mg > bg || (mg == bg && A->max_gap_start < bs))) { bg = mg; bs = A->max_gap_start; }
+    }
+    last = A->last;
+  }
+  t_first[tid] = first; t_last[tid] = last; t_bg[tid] = bg; t_bs[tid] = bs;
+#pragma unroll
+  for (int q = 0; q < 5; ++q) t_sum[q][tid] = c[q];
+  __syncthreads();
+  ReqResult* O = out + r;
+  if (tid == 0) {
+    uint64_t s5[5] = {0, 0, 0, 0, 0};
+    uint64_t f = 0, l = 0, g = 0, gs = 0;
+    for (uint32_t t = 0; t < blockDim.x; ++t) {
+#pragma unroll
+      for (int q = 0; q < 5; ++q) s5[q] += t_sum[q][t];
+      if (!t_first[t]) continue;
+      if (!f) f = t_first[t];
+      if (gaps) {
+        if (l) add_gap(t_first[t] - l, l, g, gs);
+        if (t_bg[t] && (t_bg[t] > g || (t_bg[t] == g && t_bs[t] < gs))) { g = t_bg[t]; gs = t_bs[t]; }
+      }
+      l = t_last[t];
+    }
+    O->count = s5[0]; O->c41 = s5[1]; O->c43 = s5[2]; O->c31 = s5[3]; O->c32 = s5[4];
+    O->first = f;
+    O->last = l;
+    O->max_gap = g;
+    O->max_gap_start = g ? gs : 0;
+    O->num_gaps = s5[0] ? s5[0] - 1 : 0;
+  }
+  __syncthreads();
+  for (uint32_t b = tid; b < (uint32_t)kHistBins; b += blockDim.x) {
+    uint64_t h = 0;
+    if (gaps) {
+      h = jh[b];
+      for (uint32_t j = sp.s; j < sp.e; ++j) h += ares[apos[j]].hist[b];
+    }
+    O->hist[b] = h;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host-side launchers (called by the engine)
 // ---------------------------------------------------------------------------
@@ -620,6 +703,13 @@ cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads
   }
   if (grid == 0) return cudaSuccess;
   sieve_segments_kernel<<<grid, threads, smem, stream>>>(prm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_combine(const BatchHdr* hdr, const ReqSpan* spans, const uint32_t* apos,
+                           const ReqResult* ares, ReqResult* out, uint32_t grid, cudaStream_t stream) {
+  if (grid == 0) return cudaSuccess;
+  combine_kernel<<<grid, 256, 0, stream>>>(hdr, spans, apos, ares, out);
   return cudaGetLastError();
 }
 

@@ -62,8 +62,16 @@ struct FillItem {
 // so one CUDA graph serves every batch of a slot.
 struct BatchHdr {
   uint64_t total_segs;
-  uint32_t nreq;
+  uint32_t nreq;            // device requests (atoms, when requests share work)
   uint32_t nfill;           // bucket fill items
+  uint32_t nout;            // caller requests rebuilt from atoms (0: none)
+  uint32_t pad;
+};
+
+// A caller request served from shared atoms: its atoms are [s, e) in
+// position order.
+struct ReqSpan {
+  uint32_t s, e, rflags, pad;
 };
 
 // Per segment: first/last prime (absolute, 0 = none), the largest gap

@@ -26,7 +26,8 @@ GAP_OPS = (OP_TWINS, OP_GAP_HIST)
 class ServerConfig(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
                 ("max_segments", ctypes.c_uint64), ("memory_budget", ctypes.c_uint64),
-                ("use_graphs", ctypes.c_uint32), ("bucket_bytes", ctypes.c_uint64)]
+                ("use_graphs", ctypes.c_uint32), ("bucket_bytes", ctypes.c_uint64),
+                ("isolate_requests", ctypes.c_uint32)]
 
 
 class ServerMetrics(ctypes.Structure):
@@ -54,9 +55,10 @@ for _n in ("voss_gb300_server_create", "voss_gb300_server_submit", "voss_gb300_s
 
 class Server:
     def __init__(self, slots: int = 4, max_batch: int = 256, max_segments: int = 1 << 15,
-                 memory_budget: int = 1 << 30, use_graphs: bool = True, bucket_bytes: int = 256 << 20):
+                 memory_budget: int = 1 << 30, use_graphs: bool = True, bucket_bytes: int = 256 << 20,
+                 share: bool = True):
         cfg = ServerConfig(slots, max_batch, max_segments, memory_budget, 1 if use_graphs else 0,
-                           bucket_bytes)
+                           bucket_bytes, 0 if share else 1)
         self._h = ctypes.c_void_p()
         _capi._check(_L.voss_gb300_server_create(ctypes.byref(cfg), ctypes.byref(self._h)), {})
 
