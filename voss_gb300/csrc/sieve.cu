@@ -1,24 +1,30 @@
 // sieve.cu -- wheel-30 segmented sieve with fused reductions, for sm_103a.
 //
 // One CTA owns one segment of S bytes (30*S integers) at a time, entirely in
-// shared memory, and walks a static list of (request, segment) work items.
-// Per segment:
+// shared memory, and takes (request, segment) items from a device work queue
+// (one global atomic per item; requests come heaviest first).  Per segment:
 //   1. fill: AND of two presieve tiles (primes 7..17 and 19..31) read at the
 //      segment's phase -- replaces the reference's memset + per-prime
 //      launches for the smallest primes (context.cu:404-414);
 //   2. mark with shared-memory atomicAnd, in work units handed out heaviest
 //      first by a shared counter: primes 37 <= p < split one warp each
-//      (lane = residue class x stream, fixed bit mask per stream), primes
-//      p >= split four per warp (lane = prime x class).  Each stream starts
-//      at max(p^2, segment low), as the reference's sieve_w30_seg_kernel
-//      does (sieve.cu:10-37, start offsets context.cu:354-388);
+//      (lane = residue class x stream, fixed bit mask per stream); split <=
+//      p < S four per warp-round (lane = prime x class); p >= S one lane
+//      each (at most one hit per class); primes from the request's bucket
+//      split on come from the segment's bucket list, 1024 entries per unit,
+//      read coalesced from HBM (filled by bucket_fill_kernel).  Each stream
+//      starts at max(p^2, segment low), as the reference's
+//      sieve_w30_seg_kernel does (sieve.cu:10-37, start offsets
+//      context.cu:354-388);
 //   3. reduce in the same CTA: popcount (count), masked popcount (p mod 4,
 //      p mod 3), and an ordered gap scan with a warp max-scan carrying the
 //      previous prime, histogram in shared memory -- replaces extract +
 //      thrust::sort + mod4 + gaps kernels (extract.cu:10-39,
-//      chebyshev.cu:11-25, gaps.cu:31-75).
+//      chebyshev.cu:11-25, gaps.cu:31-75).  Count-only requests skip the
+//      gap scan.
 // Segment boundaries, 2/3/5 and request totals are stitched by
-// finalize_kernel (the reference does this on the host, context.cu:462-524).
+// finalize_kernel (the reference does this on the host, context.cu:462-524);
+// combine_kernel rebuilds requests that shared atoms of a batch.
 #include <cuda_runtime.h>
 #include <cstdint>
 
