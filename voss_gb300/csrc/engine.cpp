@@ -160,27 +160,25 @@ void Engine::ensure_table(uint64_t pmax) {
   for (uint64_t i = kFirstTablePrime; i <= lim; ++i)
     if (!comp[i]) P.push_back((uint32_t)i);
   const size_t n = P.size();
-  const size_t stride = (n + 31) & ~size_t(31);
   std::vector<uint64_t> M(n);
-  std::vector<uint32_t> R(8 * stride, 0);
+  std::vector<uint32_t> R(8 * n, 0);        // the eight class residues of a prime together
   for (size_t i = 0; i < n; ++i) {
     const uint64_t p = P[i];
     M[i] = UINT64_MAX / p;
     const uint64_t inv30 = (uint64_t)inverse_mod((int64_t)(30 % p), (int64_t)p);
     for (int o = 0; o < 8; ++o)
-      R[o * stride + i] = (uint32_t)(((p - kW30[o] % p) % p) * inv30 % p);
+      R[8 * i + o] = (uint32_t)(((p - kW30[o] % p) % p) * inv30 % p);
   }
   // Plans launched earlier may still read the old table.
   check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize(table)");
   dP.reserve(std::max<size_t>(n, 1) * 4);
   dM.reserve(std::max<size_t>(n, 1) * 8);
-  dR.reserve(std::max<size_t>(stride, 32) * 8 * 4);
+  dR.reserve(std::max<size_t>(n, 1) * 8 * 4);
   if (n) {
     check_cuda(cudaMemcpy(dP.ptr, P.data(), n * 4, cudaMemcpyHostToDevice), "table P");
     check_cuda(cudaMemcpy(dM.ptr, M.data(), n * 8, cudaMemcpyHostToDevice), "table M");
     check_cuda(cudaMemcpy(dR.ptr, R.data(), R.size() * 4, cudaMemcpyHostToDevice), "table R");
   }
-  rstride = stride;
   hInvPrefix.assign(n + 1, 0.0);
   for (size_t i = 0; i < n; ++i) hInvPrefix[i + 1] = hInvPrefix[i] + 1.0 / (double)P[i];
   hP.swap(P);
@@ -516,7 +514,6 @@ void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint3
   prm.P = E.dP.as<uint32_t>();
   prm.M = E.dM.as<uint64_t>();
   prm.R = E.dR.as<uint32_t>();
-  prm.rstride = E.rstride;
   prm.tileA = E.tileA.as<uint32_t>();
   prm.tileB = E.tileB.as<uint32_t>();
   prm.seg_bytes = seg_max;
@@ -614,7 +611,6 @@ void Plan::run_device(cudaStream_t s) {
     fp.P = prm.P;
     fp.M = prm.M;
     fp.R = prm.R;
-    fp.rstride = prm.rstride;
     fp.bucket = bucket.as<uint32_t>();
     fp.bcount = bcount.as<uint32_t>();
     fp.overflow = overflow.as<unsigned int>();

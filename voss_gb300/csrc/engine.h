@@ -199,8 +199,7 @@ class Engine {
   std::vector<uint32_t> hP;
   std::vector<double> hInvPrefix;   // sum of 1/p over table primes [0, i)
   uint64_t table_limit = 0;
-  DevBuf dP, dM, dR;
-  uint64_t rstride = 0;
+  DevBuf dP, dM, dR;            // primes, Barrett constants, class residues (8 per prime)
   DevBuf tileA, tileB;
 
   // Scratch plan reused by the synchronous entry points.

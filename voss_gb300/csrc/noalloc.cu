@@ -111,7 +111,7 @@ void build_host_tables() {
     h_P[n] = i;
     h_M[n] = UINT64_MAX / p;
     const uint64_t inv30 = (uint64_t)inv_mod((int64_t)(30 % p), (int64_t)p);
-    for (int o = 0; o < 8; ++o) h_R[o * kNaStride + n] = (uint32_t)(((p - kW30h[o] % p) % p) * inv30 % p);
+    for (int o = 0; o < 8; ++o) h_R[8 * n + o] = (uint32_t)(((p - kW30h[o] % p) % p) * inv30 % p);
     ++n;
   }
   auto tile = [](uint8_t* t, uint32_t len, uint32_t period, const uint32_t* ps) {
@@ -254,7 +254,6 @@ extern "C" int voss_primes_range_stats_noalloc(uint64_t a, uint64_t b, voss_rang
   prm.P = d.P;
   prm.M = d.M;
   prm.R = d.R;
-  prm.rstride = kNaStride;
   prm.tileA = d.tileA;
   prm.tileB = d.tileB;
   prm.seg_bytes = kNaSegBytes;

@@ -63,8 +63,18 @@ __device__ __forceinline__ uint32_t lift_to_square(uint32_t s, uint64_t k0, uint
   return s2 < nbytes ? (uint32_t)s2 : nbytes;
 }
 
-__device__ __forceinline__ void clear_bit(uint32_t* seg, uint32_t j, uint32_t o) {
-  atomicAnd(seg + (j >> 2), ~(1u << (((j & 3u) << 3) | o)));
+// Clear the candidate of byte j, class o, given keep = ~(1 << o): the mask
+// is keep rotated to byte j & 3 of its word.
+__device__ __forceinline__ void clear_bit(uint32_t* seg, uint32_t j, uint32_t keep) {
+  atomicAnd(seg + (j >> 2), __funnelshift_l(keep, keep, (j & 3u) << 3));
+}
+
+// The eight class residues of table prime i (32 bytes, two vector loads).
+__device__ __forceinline__ void load_residues(const uint32_t* __restrict__ R, uint32_t i, uint32_t r[8]) {
+  const uint4 lo = __ldg(reinterpret_cast<const uint4*>(R) + 2u * i);
+  const uint4 hi = __ldg(reinterpret_cast<const uint4*>(R) + 2u * i + 1u);
+  r[0] = lo.x; r[1] = lo.y; r[2] = lo.z; r[3] = lo.w;
+  r[4] = hi.x; r[5] = hi.y; r[6] = hi.z; r[7] = hi.w;
 }
 
 struct GapSink {
@@ -221,7 +231,7 @@ sieve_segments_kernel(const SieveParams prm) {
         if (u < nsmall) {
           const uint32_t p = __ldg(prm.P + u);
           const uint32_t m = mod_barrett(k0, p, __ldg(prm.M + u));
-          const uint32_t r = __ldg(prm.R + o * prm.rstride + u);
+          const uint32_t r = __ldg(prm.R + 8u * u + o);
           uint32_t s = r >= m ? r - m : r + p - m;
           if (30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
           const uint32_t j0 = s + h * p;
@@ -241,7 +251,7 @@ sieve_segments_kernel(const SieveParams prm) {
 #pragma unroll 4
           for (uint32_t e = lane; e < lim; e += 32) {
             const uint32_t v = __ldg(prm.bucket + base + e);
-            clear_bit(seg, v & 0x3FFFFu, v >> 18);
+            clear_bit(seg, v & 0x3FFFFu, ~(1u << (v >> 18)));
           }
         } else if (u >= nsmall + nmidu) {
           // huge tier: p >= S, at most one hit per class; a lane per prime,
@@ -251,15 +261,17 @@ sieve_segments_kernel(const SieveParams prm) {
             const uint32_t p = __ldg(prm.P + i);
             const uint64_t mg = __ldg(prm.M + i);
             uint32_t rr[8];
-#pragma unroll
-            for (int t = 0; t < 8; ++t) rr[t] = __ldg(prm.R + t * prm.rstride + i);
+            load_residues(prm.R, i, rr);
             const uint32_t m = mod_barrett(k0, p, mg);
-            const bool low = 30ull * k0 < (uint64_t)p * p;
+            const uint64_t p2 = (uint64_t)p * p;
+            const bool low = 30ull * k0 < p2;
 #pragma unroll
             for (uint32_t t = 0; t < 8; ++t) {
               uint32_t s = rr[t] >= m ? rr[t] - m : rr[t] + p - m;
-              if (low) s = lift_to_square(s, k0, p, t, nbytes);
-              if (s < nbytes) clear_bit(seg, s, t);
+              // p >= the segment: s is the class's only candidate here, so
+              // below p*p there is none (the next one is s + p)
+              if (low && 30ull * (k0 + s) + w30(t) < p2) s = nbytes;
+              if (s < nbytes) clear_bit(seg, s, ~(1u << t));
             }
           }
         } else {
@@ -271,11 +283,12 @@ sieve_segments_kernel(const SieveParams prm) {
           const uint32_t pm = okm ? __ldg(prm.P + im) : 0u;
           const uint32_t mm = okm ? mod_barrett(k0, pm, __ldg(prm.M + im)) : 0u;
           const bool low_any = __any_sync(0xFFFFFFFFu, okm && 30ull * k0 < (uint64_t)pm * pm);
+          const uint32_t keep = ~(1u << o);
           uint32_t rr[8];
 #pragma unroll
           for (int t = 0; t < 8; ++t) {
             const uint32_t i = base + 4u * t + h;
-            rr[t] = i < hbeg ? __ldg(prm.R + o * prm.rstride + i) : 0u;
+            rr[t] = i < hbeg ? __ldg(prm.R + 8u * i + o) : 0u;
           }
 #pragma unroll
           for (int t = 0; t < 8; ++t) {
@@ -284,7 +297,7 @@ sieve_segments_kernel(const SieveParams prm) {
             if (!p) continue;
             uint32_t s = rr[t] >= m ? rr[t] - m : rr[t] + p - m;
             if (low_any && 30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
-            for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, o);
+            for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, keep);
           }
         }
       }
@@ -551,8 +564,7 @@ bucket_fill_kernel(const FillParams fp) {
     // first hit at or after segment g0 of each class, kept for both passes
     // (hi = none); the eight residue loads issue together
     uint32_t first[8];
-#pragma unroll
-    for (int o = 0; o < 8; ++o) first[o] = valid ? __ldg(fp.R + o * fp.rstride + i) : 0u;
+    if (valid) load_residues(fp.R, i, first);
 #pragma unroll
     for (int o = 0; o < 8; ++o) {
       uint32_t k = hi;

@@ -113,8 +113,7 @@ struct SieveParams {
   unsigned long long* queue;   // work-queue head: next (request, segment) item
   const uint32_t* P;         // table primes >= 37, ascending
   const uint64_t* M;         // floor((2^64-1)/p), for x mod p
-  const uint32_t* R;         // R[o * rstride + i]: k = R (mod p) <=> p | 30k+W30[o]
-  uint64_t rstride;
+  const uint32_t* R;         // R[8 * i + o]: k = R (mod p) <=> p | 30k+W30[o] (32 B per prime)
   const uint32_t* tileA;     // presieve tiles, extended past their period
   const uint32_t* tileB;
   uint32_t seg_bytes;        // the largest segment of the launch (shared memory)
@@ -136,7 +135,6 @@ struct FillParams {
   const uint32_t* P;
   const uint64_t* M;
   const uint32_t* R;
-  uint64_t rstride;
   uint32_t* bucket;
   uint32_t* bcount;
   unsigned int* overflow;
