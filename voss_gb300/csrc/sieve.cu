@@ -200,6 +200,7 @@ sieve_segments_kernel(const SieveParams prm) {
     {
       const uint32_t phA = (uint32_t)(k0 % kTileAPeriod);
       const uint32_t phB = (uint32_t)(k0 % kTileBPeriod);
+#pragma unroll 4
       for (uint32_t w = tid; w < nwords; w += nthr)
         seg[w] = tile_word(prm.tileA, phA + 4u * w) & tile_word(prm.tileB, phB + 4u * w);
     }
