@@ -110,6 +110,71 @@ __device__ __forceinline__ void record_gap(const GapSink& sk, uint32_t vprev, ui
   }
 }
 
+// A claimed (request, segment) work item with what the CTA needs of it.
+struct SegItem {
+  uint64_t item, k0, seg_in_req, bbase;
+  uint32_t req, nbytes, np, split, huge, rflags, bcnt, valid;
+};
+
+// Number of leading i in [0, n) for which pred(i) holds (pred holds on a
+// prefix), by a 32-ary search of one warp: each step probes 32 evenly spaced
+// points, so about log32(n) dependent loads instead of log2(n).
+template <class Pred>
+__device__ __forceinline__ uint32_t warp_count_leading(uint32_t n, uint32_t lane, Pred pred) {
+  uint32_t lo = 0, hi = n;                      // the answer is in [lo, hi]
+  while (lo < hi) {
+    const uint32_t step = (hi - lo + 31u) / 32u;
+    const uint32_t idx = lo + lane * step;
+    const bool t = idx < hi && pred(idx);
+    const uint32_t k = (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, t));
+    if (k == 0) break;                          // pred(lo) fails: the answer is lo
+    const uint32_t last_true = lo + (k - 1u) * step;
+    hi = min(hi, lo + k * step);                // first probe that failed (or the end)
+    lo = last_true + 1u;
+  }
+  return lo;
+}
+
+// Claim the next work item and look it up, by one whole warp: its request
+// (the last with seg_base <= item), its bytes, the table primes with p*p
+// below its upper end, and its bucket list.  Lane 0 writes d.
+__device__ __noinline__ void claim_item(unsigned long long* queue, const ReqDesc* __restrict__ reqs,
+                                        const uint32_t* __restrict__ P, const uint32_t* __restrict__ bcount,
+                                        uint64_t total_segs, uint32_t nreq, SegItem& d, uint32_t lane) {
+  unsigned long long it = 0;
+  if (lane == 0) it = atomicAdd(queue, 1ull);
+  const uint64_t item = __shfl_sync(0xFFFFFFFFu, it, 0);
+  if (item >= total_segs) {
+    if (lane == 0) { d.item = item; d.valid = 0; }
+    return;
+  }
+  const uint32_t r = warp_count_leading(nreq, lane, [&](uint32_t i) { return reqs[i].seg_base <= item; }) - 1u;
+  const ReqDesc& R = reqs[r];
+  const uint64_t si = item - R.seg_base;
+  const uint64_t k0 = R.k_lo + si * R.seg_bytes;
+  const uint64_t left = R.k_hi - k0;
+  const uint32_t nb = left < R.seg_bytes ? (uint32_t)left : R.seg_bytes;
+  const uint64_t hi_num = 30ull * (k0 + nb);
+  // only primes up to the bucket split matter (the rest come from the list)
+  const uint32_t lim = R.bucket_idx < R.nprimes ? R.bucket_idx + 1u : R.nprimes;
+  uint32_t a = warp_count_leading(lim, lane, [&](uint32_t i) {
+    const uint64_t p = P[i];
+    return p * p < hi_num;
+  });
+  if (lane == 0) {
+    d.bcnt = 0;
+    d.bbase = 0;
+    if (R.bucket_idx < a) {
+      a = R.bucket_idx;
+      d.bcnt = min(bcount[item], R.bucket_cap);
+      d.bbase = R.bucket_base + si * (uint64_t)R.bucket_cap;
+    }
+    d.item = item; d.valid = 1;
+    d.req = r; d.k0 = k0; d.seg_in_req = si; d.nbytes = nb; d.np = a;
+    d.split = R.tier_split; d.huge = R.tier_huge; d.rflags = R.rflags;
+  }
+}
+
 // Shared-memory per-warp record used to stitch warps inside a segment.
 struct WarpRec {
   uint32_t first1, last1;    // relative value + 1 (0 = none)
@@ -125,9 +190,10 @@ sieve_segments_kernel(const SieveParams prm) {
   uint32_t* shist = seg + (prm.seg_bytes >> 2);
   WarpRec* wrec = reinterpret_cast<WarpRec*>(shist + kSmemHistCopies * kSmemStride);
 
-  __shared__ uint64_t s_k0, s_seg_in_req, s_item;
-  __shared__ uint32_t s_req, s_nbytes, s_np, s_ctr, s_split, s_huge, s_rflags, s_bcnt;
-  __shared__ uint64_t s_bbase;
+  // the segment in hand, and the next one, claimed and looked up by thread 0
+  // while the others mark (so no thread waits on that lookup)
+  __shared__ SegItem s_cur, s_nxt;
+  __shared__ uint32_t s_ctr;
   __shared__ uint32_t s_vtab[32];      // bit b of a word -> 30*(b/8) + W30[b%8]
 
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -140,49 +206,19 @@ sieve_segments_kernel(const SieveParams prm) {
 
   const uint64_t total_segs = prm.hdr->total_segs;
   const uint32_t nreq = prm.hdr->nreq;
+  if (warp == 0) claim_item(prm.queue, prm.reqs, prm.P, prm.bcount, total_segs, nreq, s_nxt, lane);
   for (;;) {
     // work queue: the next (request, segment) item, heaviest requests first
-    if (tid == 0) s_item = atomicAdd(prm.queue, 1ull);
     __syncthreads();
-    const uint64_t item = s_item;
-    if (item >= total_segs) break;
-    if (tid == 0) {
-      uint32_t lo = 0, hi = nreq;                 // last request with seg_base <= item
-      while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (prm.reqs[mid].seg_base <= item) lo = mid; else hi = mid;
-      }
-      const ReqDesc& R = prm.reqs[lo];
-      const uint64_t si = item - R.seg_base;
-      const uint64_t k0 = R.k_lo + si * R.seg_bytes;
-      const uint64_t left = R.k_hi - k0;
-      const uint32_t nb = left < R.seg_bytes ? (uint32_t)left : R.seg_bytes;
-      s_split = R.tier_split;
-      s_huge = R.tier_huge;
-      s_rflags = R.rflags;
-      // table primes with p*p below the segment's upper end
-      const uint64_t hi_num = 30ull * (k0 + nb);
-      uint32_t a = 0, b = R.nprimes;
-      while (a < b) {
-        const uint32_t mid = (a + b) >> 1;
-        const uint64_t p = prm.P[mid];
-        if (p * p < hi_num) a = mid + 1; else b = mid;
-      }
-      // primes from bucket_idx on come from this segment's bucket list
-      s_bcnt = 0;
-      if (R.bucket_idx < a) {
-        a = R.bucket_idx;
-        s_bcnt = min(prm.bcount[item], R.bucket_cap);
-        s_bbase = R.bucket_base + si * (uint64_t)R.bucket_cap;
-      }
-      s_req = lo; s_k0 = k0; s_seg_in_req = si; s_nbytes = nb; s_np = a;
-    }
+    if (tid == 0) s_cur = s_nxt;
     __syncthreads();
-    const uint32_t req = s_req;
-    const uint64_t k0 = s_k0;
-    const uint32_t nbytes = s_nbytes;
+    if (!s_cur.valid) break;
+    const uint64_t item = s_cur.item;
+    const uint32_t req = s_cur.req;
+    const uint64_t k0 = s_cur.k0;
+    const uint32_t nbytes = s_cur.nbytes;
     const uint32_t nwords = (nbytes + 3u) >> 2;
-    const uint32_t np = s_np;
+    const uint32_t np = s_cur.np;
 
     if ((int)req != cur_req) {
       if (cur_req >= 0) {                           // flush the previous request's bins
@@ -216,12 +252,14 @@ sieve_segments_kernel(const SieveParams prm) {
     {
       // unit layout: [0, nsmall) small primes, then 32-prime units of the mid
       // tier (split <= p < S), then 32-prime units of the huge tier (p >= S)
-      const uint32_t nsmall = s_split < np ? s_split : np;
-      const uint32_t hbeg = s_huge < np ? max(s_huge, nsmall) : np;
+      const uint32_t nsmall = s_cur.split < np ? s_cur.split : np;
+      const uint32_t hbeg = s_cur.huge < np ? max(s_cur.huge, nsmall) : np;
       const uint32_t nmidu = (hbeg - nsmall + 31u) / 32u;
       const uint32_t nhugeu = (np - hbeg + 31u) / 32u;
       const uint32_t nscan = nsmall + nmidu + nhugeu;
-      const uint32_t bcnt = s_bcnt;
+      const uint32_t bcnt = s_cur.bcnt;
+      const uint64_t bbase = s_cur.bbase;
+      if (warp == 0) claim_item(prm.queue, prm.reqs, prm.P, prm.bcount, total_segs, nreq, s_nxt, lane);   // overlaps the marking
       const uint32_t nunits = nscan + (bcnt + kBucketUnit - 1) / kBucketUnit;
       const uint32_t o = lane & 7u, h = lane >> 3;
       for (;;) {
@@ -247,7 +285,7 @@ sieve_segments_kernel(const SieveParams prm) {
         } else if (u >= nscan) {
           // bucket list of this segment: primes >= the bucket split whose
           // hits were listed by bucket_fill_kernel; entries read coalesced
-          const uint64_t base = s_bbase + (uint64_t)(u - nscan) * kBucketUnit;
+          const uint64_t base = bbase + (uint64_t)(u - nscan) * kBucketUnit;
           const uint32_t lim = min(kBucketUnit, bcnt - (u - nscan) * kBucketUnit);
 #pragma unroll 8
           for (uint32_t e = lane; e < lim; e += 32) {
@@ -312,7 +350,7 @@ sieve_segments_kernel(const SieveParams prm) {
       // The tiles clear their own primes: 7..29 live in byte 0, 31 in byte 1.
       if (k0 == 0) seg[0] = (seg[0] & 0xFFFFFE00u) | 0x1FEu;   // 1 no; 7..29, 31 yes
       else if (k0 == 1) seg[0] |= 1u;                            // 31
-      if (s_seg_in_req == 0) {
+      if (s_cur.seg_in_req == 0) {
         uint32_t m = 0;
         for (uint32_t o = 0; o < 8; ++o) if (30ull * k0 + w30(o) < R.a) m |= 1u << o;
         seg[0] &= ~m;
@@ -348,7 +386,7 @@ sieve_segments_kernel(const SieveParams prm) {
       const uint32_t wbeg = min(tid * run, nwords);
       const uint32_t wend = min(wbeg + run, nwords);
       uint32_t first1 = 0, last1 = 0, cnt = 0, c41 = 0, c31 = 0, maxg = 0, maxgs = 0;
-      const bool gaps = (s_rflags & kReqGaps) != 0;
+      const bool gaps = (s_cur.rflags & kReqGaps) != 0;
       for (uint32_t wi = wbeg; wi < wend; ++wi) {
         uint32_t w = seg[wi];
         if (!w) continue;
