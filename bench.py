@@ -227,7 +227,7 @@ def secondary(torch, stream, flush):
     return out
 
 
-def serving(torch, n=2000):
+def serving(torch, n=100000):
     """Served (continuous batching) vs plain one-call-per-request, same stream."""
     from voss_gb300.serve import Server, run_plain, run_served, same_answer, serving_mix
     reqs = serving_mix(n)
