@@ -67,7 +67,12 @@ constexpr int kGbThreads = 256;
 constexpr int kGbWords = 4;                                  // U words per thread
 constexpr uint32_t kGbTile = kGbThreads * kGbWords * 32;     // even n per tile
 constexpr uint32_t kGbSmemHist = 4096;                       // p < 4096 counted in smem
-constexpr size_t kGbSmemBytes = kGbSmemHist * 4 + kGbTile * 2;
+constexpr size_t kGbSmemBytes = kGbSmemHist * 4;
+// Zero words before and after the odd-number bitmap: a thread's five window
+// words (floor(base/32) + 4*tid .. + 4) then never leave the buffer, with no
+// bounds test (base >= -16382 in the first tile; the last tile's window ends
+// at most kGbTile/32 + 1 words past the bitmap).
+constexpr uint64_t kGbPad = 1088;
 
 struct GbOut {
   uint32_t* minp;                    // optional, index (n-4)/2
@@ -81,31 +86,30 @@ struct GbOut {
   unsigned int* err;                 // 1: the prime list ran out before n/2
 };
 
-__global__ void __launch_bounds__(kGbThreads, 2)
-goldbach_minp_kernel(const uint32_t* __restrict__ odd, uint64_t odd_words,
+__global__ void __launch_bounds__(kGbThreads, 4)
+goldbach_minp_kernel(const uint32_t* __restrict__ odd,
                      const uint32_t* __restrict__ oddp, uint32_t noddp, uint64_t N,
                      uint64_t ntiles, GbOut out) {
   extern __shared__ __align__(16) uint32_t gb_smem[];
   uint32_t* shist = gb_smem;                                          // kGbSmemHist
-  uint16_t* sminp = reinterpret_cast<uint16_t*>(gb_smem + kGbSmemHist);  // kGbTile
-  const uint32_t tid = threadIdx.x;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u;
   const uint64_t n_last = N & ~1ull;           // largest even n
   uint32_t lmax = 0;
   unsigned long long lsum = 0, lprobes = 0;
   for (uint32_t i = tid; i < kGbSmemHist; i += kGbThreads) shist[i] = 0;
+  __syncthreads();
 
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint64_t n0 = 6 + tile * 2ull * kGbTile;
     const uint64_t nmax = umin64(n_last, n0 + 2ull * (kGbTile - 1));
     const uint32_t tcount = (uint32_t)((nmax - n0) / 2 + 1);
-    for (uint32_t i = tid; i < kGbTile; i += kGbThreads) sminp[i] = 0;
+    const uint64_t obase = 1 + tile * (uint64_t)kGbTile;     // (n0 - 4) / 2
     uint32_t U[kGbWords];
 #pragma unroll
     for (int q = 0; q < kGbWords; ++q) {
       const uint32_t t0 = 32u * (tid * kGbWords + q);
       U[q] = t0 >= tcount ? 0u : (tcount - t0 >= 32 ? 0xFFFFFFFFu : ((1u << (tcount - t0)) - 1u));
     }
-    __syncthreads();
     bool exhausted = true;
     for (uint32_t pi = 0; pi < noddp; ++pi) {
       const uint32_t p = __ldg(oddp + pi);
@@ -113,27 +117,41 @@ goldbach_minp_kernel(const uint32_t* __restrict__ odd, uint64_t odd_words,
       if ((pi & 7u) == 0) {
         if (!__syncthreads_or((U[0] | U[1] | U[2] | U[3]) != 0)) { exhausted = false; break; }
       }
-      const int64_t base = ((int64_t)n0 - (int64_t)p - 1) / 2;   // odd-bit index at t = 0
+      // bit j of this thread's word q is n = n0 + 2*(32*(4*tid + q) + j); its
+      // partner n - p is odd bit base + 32*(4*tid + q) + j, so the thread's
+      // four windows are five consecutive bitmap words shifted by base mod 32
+      const int64_t base = ((int64_t)n0 - (int64_t)p - 1) / 2;   // exact: n0 even, p odd
+      uint32_t nres = 0;
+      if (U[0] | U[1] | U[2] | U[3]) {
+        const uint32_t* wp = odd + ((base >> 5) + (int64_t)(kGbWords * tid));
+        const uint32_t sh = (uint32_t)base & 31u;
+        uint32_t a[kGbWords + 1];
 #pragma unroll
-      for (int q = 0; q < kGbWords; ++q) {
-        if (!U[q]) continue;
-        const uint32_t w = tid * kGbWords + q;
-        const int64_t bi = base + 32ll * w;
-        const int64_t wi = bi >> 5;                               // floor
-        const uint32_t sh = (uint32_t)(bi & 31);
-        const uint32_t lo = (wi >= 0 && (uint64_t)wi < odd_words) ? __ldg(odd + wi) : 0u;
-        const uint32_t hi = (wi + 1 >= 0 && (uint64_t)(wi + 1) < odd_words) ? __ldg(odd + wi + 1) : 0u;
-        const uint32_t win = __funnelshift_r(lo, hi, sh);
-        uint32_t hit = U[q] & win;
-        ++lprobes;
-        if (hit) {
+        for (int q = 0; q <= kGbWords; ++q) a[q] = __ldg(wp + q);
+#pragma unroll
+        for (int q = 0; q < kGbWords; ++q) {
+          if (!U[q]) continue;
+          ++lprobes;
+          uint32_t hit = U[q] & __funnelshift_r(a[q], a[q + 1], sh);
+          if (!hit) continue;
           U[q] &= ~hit;
-          do {
-            const uint32_t j = (uint32_t)__ffs(hit) - 1u;
-            hit &= hit - 1u;
-            sminp[32u * w + j] = (uint16_t)p;
-          } while (hit);
+          nres += __popc(hit);
+          if (out.minp) {
+            const uint64_t o = obase + 32u * (tid * kGbWords + q);
+            do {
+              const uint32_t j = (uint32_t)__ffs(hit) - 1u;
+              hit &= hit - 1u;
+              out.minp[o + j] = p;
+            } while (hit);
+          }
         }
+      }
+      // the n resolved at p, per warp: one histogram update
+      if (nres) { lmax = max(lmax, p); lsum += (unsigned long long)p * nres; }
+      const uint32_t wres = __reduce_add_sync(0xFFFFFFFFu, nres);
+      if (lane == 0 && wres) {
+        if (p < kGbSmemHist) atomicAdd(&shist[p], wres);
+        else atomicAdd(&out.hist[p], (unsigned long long)wres);
       }
     }
     // Whatever is left: counterexamples, unless the prime list ran out first.
@@ -150,23 +168,12 @@ goldbach_minp_kernel(const uint32_t* __restrict__ odd, uint64_t odd_words,
         if (slot < out.ce_cap) out.ce[slot] = n;
       }
     }
-    __syncthreads();
-    const uint64_t obase = 1 + tile * (uint64_t)kGbTile;     // (n0 - 4) / 2
-    for (uint32_t i = tid; i < tcount; i += kGbThreads) {
-      const uint32_t p = sminp[i];
-      if (out.minp) out.minp[obase + i] = p;
-      lmax = max(lmax, p);
-      lsum += p;
-      if (p < kGbSmemHist) atomicAdd(&shist[p], 1u);
-      else atomicAdd(&out.hist[p], 1ull);
-    }
-    __syncthreads();
   }
+  __syncthreads();
   for (uint32_t i = tid; i < kGbSmemHist; i += kGbThreads)
     if (shist[i]) atomicAdd(&out.hist[i], (unsigned long long)shist[i]);
-  // counterexamples contributed p = 0 to hist[0]; harmless, the host ignores bin 0
   lmax = __reduce_max_sync(0xFFFFFFFFu, lmax);
-  if ((tid & 31) == 0) atomicMax(out.max_minp, lmax);
+  if (lane == 0) atomicMax(out.max_minp, lmax);
   atomicAdd(out.sum_minp, lsum);
   atomicAdd(out.probes, lprobes);
 }
@@ -298,13 +305,17 @@ GoldbachPlan* goldbach_plan_create(Engine& E, uint64_t N) {
   g->oddp.reserve(op.size() * 4);
   check_cuda(cudaMemcpy(g->oddp.ptr, op.data(), op.size() * 4, cudaMemcpyHostToDevice), "odd primes");
   g->odd_words = (N / 2 + 1 + 31) / 32 + 2;
-  g->odd.reserve(g->odd_words * 4);
+  g->odd.reserve((g->odd_words + 2 * kGbPad) * 4);
   g->hist.reserve(sizeof(unsigned long long) * kGoldbachHistBins);
   g->scalars.reserve(64);
   g->ce_cap = 1024;
   g->ce.reserve(8 * g->ce_cap);
   g->ntiles = N >= 6 ? ((N & ~1ull) - 6) / (2ull * kGbTile) + 1 : 0;
-  g->grid = (uint32_t)std::min<uint64_t>(g->ntiles, (uint64_t)E.sm_count * 2);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, goldbach_minp_kernel, kGbThreads, kGbSmemBytes) !=
+          cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  g->grid = (uint32_t)std::min<uint64_t>(g->ntiles, (uint64_t)E.sm_count * per_sm);
   g->sieve.eng = &E;
   return g.release();
 }
@@ -318,11 +329,16 @@ void goldbach_plan_launch(GoldbachPlan* g, cudaStream_t s) {
     g->sieve.launch(s);
   }
   const uint32_t* wb = g->sieve.bitmap.as<uint32_t>();
-  odd_bitmap_kernel<<<E.sm_count * 8, 256, 0, s>>>(wb, g->odd.as<uint32_t>(), g->odd_words - 2, g->N);
+  uint32_t* odd = g->odd.as<uint32_t>() + kGbPad;
+  odd_bitmap_kernel<<<E.sm_count * 8, 256, 0, s>>>(wb, odd, g->odd_words - 2, g->N);
   check_cuda(cudaGetLastError(), "odd_bitmap_kernel");
-  check_cuda(cudaMemsetAsync(g->odd.as<uint32_t>() + (g->odd_words - 2), 0, 8, s), "odd pad");
+  check_cuda(cudaMemsetAsync(g->odd.as<uint32_t>(), 0, 4 * kGbPad, s), "odd pad");
+  check_cuda(cudaMemsetAsync(odd + (g->odd_words - 2), 0, 4 * (2 + kGbPad), s), "odd pad");
   check_cuda(cudaMemsetAsync(g->hist.ptr, 0, sizeof(unsigned long long) * kGoldbachHistBins, s), "hist");
   check_cuda(cudaMemsetAsync(g->scalars.ptr, 0, 64, s), "scalars");
+  // n never resolved (a counterexample) keep min p = 0
+  if (g->want_minp)
+    check_cuda(cudaMemsetAsync(g->minp.ptr, 0, 4 * ((g->N - 4) / 2 + 1), s), "minp");
   if (!g->ntiles) return;
   auto* sc = g->scalars.as<unsigned long long>();
   GbOut o;
@@ -341,9 +357,8 @@ void goldbach_plan_launch(GoldbachPlan* g, cudaStream_t s) {
                                     (int)kGbSmemBytes), "goldbach smem");
     attr_set = true;
   }
-  goldbach_minp_kernel<<<g->grid, kGbThreads, kGbSmemBytes, s>>>(g->odd.as<uint32_t>(), g->odd_words,
-                                                      g->oddp.as<uint32_t>(), kGoldbachPrimes,
-                                                      g->N, g->ntiles, o);
+  goldbach_minp_kernel<<<g->grid, kGbThreads, kGbSmemBytes, s>>>(odd, g->oddp.as<uint32_t>(), kGoldbachPrimes,
+                                                                  g->N, g->ntiles, o);
   check_cuda(cudaGetLastError(), "goldbach_minp_kernel");
 }
 
