@@ -28,9 +28,6 @@ namespace vg {
 
 namespace {
 
-__constant__ uint8_t kClassOf[30] = {
-    0xFF, 0, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 1, 0xFF, 0xFF, 0xFF, 2, 0xFF, 3, 0xFF,
-    0xFF, 0xFF, 4, 0xFF, 5, 0xFF, 0xFF, 0xFF, 6, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 7};
 
 __device__ __forceinline__ uint64_t umin64(uint64_t x, uint64_t y) { return x < y ? x : y; }
 
@@ -39,26 +36,37 @@ __device__ __forceinline__ uint32_t wheel_bit(const uint32_t* __restrict__ wb, u
   return (__ldg(wb + (k >> 2)) >> ((uint32_t)((k & 3) << 3) + o)) & 1u;
 }
 
-// Odd-number bitmap: bit i of `odd` <-> 2i+1, for 2i+1 <= limit.
-__global__ void odd_bitmap_kernel(const uint32_t* __restrict__ wb, uint32_t* __restrict__ odd,
-                                  uint64_t odd_words, uint64_t limit) {
+// Odd-number bitmap: bit i of `odd` <-> 2i+1, for 2i+1 <= limit.  Byte k of
+// the wheel bitmap holds the odd numbers 30k+1 .. 30k+29, which are odd bits
+// 15k .. 15k+14, its class o at offset (W30[o]-1)/2 = 0,3,5,6,8,9,11,14; a
+// 256-entry table spreads a byte to its 15-bit chunk, and an output word (odd
+// bits 32w .. 32w+31) is at most four chunks shifted into place.  3 and 5 are
+// not wheel residues and are set by hand.  Wheel bytes from kbytes on are 0.
+__global__ void odd_bitmap_kernel(const uint32_t* __restrict__ wb, uint64_t kbytes,
+                                  uint32_t* __restrict__ odd, uint64_t odd_words, uint64_t limit) {
+  __shared__ uint16_t lut[256];
+  constexpr uint32_t kOddOffsets = 0xEB986530u;      // (W30[o]-1)/2, 4 bits per class
+  for (uint32_t v = threadIdx.x; v < 256; v += blockDim.x) {
+    uint32_t c = 0;
+    for (uint32_t o = 0; o < 8; ++o)
+      if ((v >> o) & 1u) c |= 1u << ((kOddOffsets >> (4 * o)) & 15u);
+    lut[v] = (uint16_t)c;
+  }
+  __syncthreads();
+  const uint8_t* __restrict__ bytes = reinterpret_cast<const uint8_t*>(wb);
   for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < odd_words;
        w += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t m0 = 64 * w + 1;
-    uint64_t k = m0 / 30;
-    uint32_t r = (uint32_t)(m0 - 30 * k);
-    uint32_t out = 0;
-    for (uint32_t j = 0; j < 32; ++j) {
-      const uint64_t m = m0 + 2 * j;
-      if (m > limit) break;
-      const uint32_t c = kClassOf[r];
-      uint32_t bit;
-      if (c != 0xFF) bit = wheel_bit(wb, k, c);
-      else bit = (m == 3 || m == 5);
-      out |= bit << j;
-      r += 2;
-      if (r >= 30) { r -= 30; ++k; }
+    const uint64_t b0 = 32 * w;
+    const uint64_t k0 = b0 / 15;
+    const uint32_t off = (uint32_t)(b0 - 15 * k0);
+    uint64_t acc = 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const uint64_t k = k0 + c;
+      if (k < kbytes) acc |= (uint64_t)lut[__ldg(bytes + k)] << (15 * c);
     }
+    uint32_t out = (uint32_t)(acc >> off);
+    if (w == 0) out |= (limit >= 3 ? 2u : 0u) | (limit >= 5 ? 4u : 0u);
     odd[w] = out;
   }
 }
@@ -330,7 +338,8 @@ void goldbach_plan_launch(GoldbachPlan* g, cudaStream_t s) {
   }
   const uint32_t* wb = g->sieve.bitmap.as<uint32_t>();
   uint32_t* odd = g->odd.as<uint32_t>() + kGbPad;
-  odd_bitmap_kernel<<<E.sm_count * 8, 256, 0, s>>>(wb, odd, g->odd_words - 2, g->N);
+  const uint64_t kbytes = (g->N + 1 + 29) / 30;          // wheel bytes of [0, N]
+  odd_bitmap_kernel<<<E.sm_count * 8, 256, 0, s>>>(wb, kbytes, odd, g->odd_words - 2, g->N);
   check_cuda(cudaGetLastError(), "odd_bitmap_kernel");
   check_cuda(cudaMemsetAsync(g->odd.as<uint32_t>(), 0, 4 * kGbPad, s), "odd pad");
   check_cuda(cudaMemsetAsync(odd + (g->odd_words - 2), 0, 4 * (2 + kGbPad), s), "odd pad");
