@@ -72,15 +72,24 @@ __global__ void odd_bitmap_kernel(const uint32_t* __restrict__ wb, uint64_t kbyt
 }
 
 constexpr int kGbThreads = 256;
-constexpr int kGbWords = 4;                                  // U words per thread
+constexpr int kGbWords = 8;                                  // U words per thread
 constexpr uint32_t kGbTile = kGbThreads * kGbWords * 32;     // even n per tile
 constexpr uint32_t kGbSmemHist = 4096;                       // p < 4096 counted in smem
 constexpr size_t kGbSmemBytes = kGbSmemHist * 4;
-// Zero words before and after the odd-number bitmap: a thread's five window
-// words (floor(base/32) + 4*tid .. + 4) then never leave the buffer, with no
-// bounds test (base >= -16382 in the first tile; the last tile's window ends
-// at most kGbTile/32 + 1 words past the bitmap).
-constexpr uint64_t kGbPad = 1088;
+// Zero words before and after the odd-number bitmap: a thread's window words
+// (floor(base/32) + kGbWords*tid .. + kGbWords) then never leave the buffer,
+// with no bounds test (base >= -kGbTile/2 in the first tile, so at most
+// kGbTile/64 words before it; the last tile's window ends at most
+// kGbTile/32 + 1 words past the bitmap).
+constexpr uint64_t kGbPad = kGbTile / 32 + 64;
+
+// Does any of this thread's n wait for a prime?
+__device__ __forceinline__ bool any_open(const uint32_t (&U)[kGbWords]) {
+  uint32_t x = 0;
+#pragma unroll
+  for (int q = 0; q < kGbWords; ++q) x |= U[q];
+  return x != 0;
+}
 
 struct GbOut {
   uint32_t* minp;                    // optional, index (n-4)/2
@@ -123,14 +132,14 @@ goldbach_minp_kernel(const uint32_t* __restrict__ odd,
       const uint32_t p = __ldg(oddp + pi);
       if (2ull * p > nmax) { exhausted = false; break; }
       if ((pi & 7u) == 0) {
-        if (!__syncthreads_or((U[0] | U[1] | U[2] | U[3]) != 0)) { exhausted = false; break; }
+        if (!__syncthreads_or(any_open(U))) { exhausted = false; break; }
       }
       // bit j of this thread's word q is n = n0 + 2*(32*(4*tid + q) + j); its
       // partner n - p is odd bit base + 32*(4*tid + q) + j, so the thread's
       // four windows are five consecutive bitmap words shifted by base mod 32
       const int64_t base = ((int64_t)n0 - (int64_t)p - 1) / 2;   // exact: n0 even, p odd
       uint32_t nres = 0;
-      if (U[0] | U[1] | U[2] | U[3]) {
+      if (any_open(U)) {
         const uint32_t* wp = odd + ((base >> 5) + (int64_t)(kGbWords * tid));
         const uint32_t sh = (uint32_t)base & 31u;
         uint32_t a[kGbWords + 1];
