@@ -60,6 +60,19 @@ int voss_primes_range_stats_ex(uint64_t a, uint64_t b, voss_range_stats_t* out,
 int voss_primes_range_stats_batch(uint64_t n, const uint64_t* a, const uint64_t* b,
                                   voss_range_stats_t* out);
 
+/* How a batch shares work (voss_primes_range_stats_batch and the server):
+ * the ranges [a[i], b[i]) cut at every endpoint into the disjoint pieces
+ * that some range covers, ascending.  Writes *npieces, the pieces
+ * [piece_a[j], piece_b[j]) and piece_gaps[j] (1 if a range over the piece
+ * has gaps_wanted[i] != 0, or gaps_wanted is NULL), and for each range the
+ * pieces [first[i], last[i]) that tile it (0, 0 for an empty range).  cap is
+ * the room in the piece arrays; 2n - 1 always suffices.  Host only: runs
+ * without a GPU. */
+int voss_gb300_cut_ranges(uint64_t n, const uint64_t* a, const uint64_t* b,
+                          const uint32_t* gaps_wanted, uint64_t cap, uint64_t* piece_a,
+                          uint64_t* piece_b, uint32_t* piece_gaps, uint64_t* npieces,
+                          uint32_t* first, uint32_t* last);
+
 /* voss_primes_range_stats for callers that cannot allocate device memory
  * while they run -- for instance a process whose device memory belongs to
  * another framework's caching allocator, or a latency-critical loop where

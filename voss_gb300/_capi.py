@@ -122,6 +122,8 @@ _SIGS = {
     "voss_gb300_goldbach_results": ([vp, P(u32), P(u64), P(u64), P(u64), P(u64), vp], c_int),
     "voss_gb300_goldbach_free": ([vp], None),
     "voss_gb300_device_info": ([ctypes.c_char_p, u32, P(u32)], c_int),
+    "voss_gb300_cut_ranges": ([u64, P(u64), P(u64), P(u32), u64, P(u64), P(u64), P(u32), P(u64),
+                               P(u32), P(u32)], c_int),
 }
 
 for _name, (_args, _res) in _SIGS.items():

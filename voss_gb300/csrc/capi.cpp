@@ -630,6 +630,37 @@ extern "C" int voss_primes_range_stats_batch(uint64_t n, const uint64_t* a, cons
   }, VOSS_ERR_INTERNAL);
 }
 
+extern "C" int voss_gb300_cut_ranges(uint64_t n, const uint64_t* a, const uint64_t* b,
+                                     const uint32_t* gaps_wanted, uint64_t cap, uint64_t* piece_a,
+                                     uint64_t* piece_b, uint32_t* piece_gaps, uint64_t* npieces,
+                                     uint32_t* first, uint32_t* last) {
+  if (!npieces || (n && (!a || !b || !first || !last))) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+  if (n > 0x7FFFFFFFull) { set_err("too many ranges"); return VOSS_ERR_INVALID_ARG; }
+  *npieces = 0;
+  if (n == 0) return VOSS_OK;
+  return guarded([&] {
+    std::vector<uint32_t> rf;
+    if (gaps_wanted) {
+      rf.resize(n);
+      for (uint64_t i = 0; i < n; ++i) rf[i] = gaps_wanted[i] ? vg::kReqGaps : 0u;
+    }
+    std::vector<uint64_t> pa, pb;
+    std::vector<uint32_t> pr;
+    std::vector<vg::ReqSpan> sp;
+    vg::cut_ranges((uint32_t)n, a, b, gaps_wanted ? rf.data() : nullptr, pa, pb, pr, sp);
+    *npieces = pa.size();
+    if (pa.size() > cap) { set_err("piece arrays too small (2n - 1 always suffices)"); return VOSS_ERR_INVALID_ARG; }
+    if (!pa.empty() && (!piece_a || !piece_b)) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+    for (size_t j = 0; j < pa.size(); ++j) {
+      piece_a[j] = pa[j];
+      piece_b[j] = pb[j];
+      if (piece_gaps) piece_gaps[j] = (pr[j] & vg::kReqGaps) ? 1u : 0u;
+    }
+    for (uint64_t i = 0; i < n; ++i) { first[i] = sp[i].s; last[i] = sp[i].e; }
+    return VOSS_OK;
+  }, VOSS_ERR_INTERNAL);
+}
+
 extern "C" int voss_gb300_get_config(voss_gb300_config_t* out) {
   if (!out) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
   return guarded([&] {

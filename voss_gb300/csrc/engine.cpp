@@ -307,22 +307,19 @@ uint64_t Plan::segments_for(uint64_t a, uint64_t b) const {
   return (bytes + c.seg_bytes - 1) / c.seg_bytes;
 }
 
-void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
-                const uint32_t* rflags) {
-  nout = 0;
-  if (!share || (fl & kFlagBitmap)) {
-    load_requests(n, a, b, fl, rflags);
-    return;
-  }
-  if (cap_out && n > cap_out) throw Error(VOSS_ERR_INVALID_ARG, "batch exceeds the plan's capacity");
-  // Cut the ranges at every endpoint; keep the pieces some request covers.
+void cut_ranges(uint32_t n, const uint64_t* a, const uint64_t* b, const uint32_t* rflags,
+                std::vector<uint64_t>& atom_a, std::vector<uint64_t>& atom_b,
+                std::vector<uint32_t>& atom_rf, std::vector<ReqSpan>& spans) {
+  // every endpoint, once, in order; the elementary pieces lie between them
   std::vector<uint64_t> pts;
-  pts.reserve(2 * n);
+  pts.reserve(2 * (size_t)n);
   for (uint32_t i = 0; i < n; ++i)
     if (b[i] > a[i]) { pts.push_back(a[i]); pts.push_back(b[i]); }
   std::sort(pts.begin(), pts.end());
   pts.erase(std::unique(pts.begin(), pts.end()), pts.end());
   const size_t np = pts.size();
+  // coverage of each piece (all requests, and those that want gaps) by
+  // difference arrays over the endpoints
   std::vector<int32_t> cov(np + 1, 0), gcov(np + 1, 0);
   auto at = [&](uint64_t x) { return (size_t)(std::lower_bound(pts.begin(), pts.end(), x) - pts.begin()); };
   for (uint32_t i = 0; i < n; ++i) {
@@ -337,13 +334,32 @@ void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
   for (size_t k = 0; k + 1 < np; ++k) {
     c += cov[k];
     g += gcov[k];
-    if (c > 0) {
+    if (c > 0) {                                      // covered pieces become atoms
       atom_of[k] = (uint32_t)atom_a.size();
       atom_a.push_back(pts[k]);
       atom_b.push_back(pts[k + 1]);
       atom_rf.push_back(g > 0 ? kReqGaps : 0u);
     }
   }
+  spans.assign(n, ReqSpan{0, 0, 0, 0});
+  for (uint32_t i = 0; i < n; ++i) {
+    spans[i].rflags = rflags ? rflags[i] : kReqGaps;
+    if (b[i] <= a[i]) continue;
+    // every piece inside the request is covered, so its atoms are contiguous
+    spans[i].s = atom_of[at(a[i])];
+    spans[i].e = atom_of[at(b[i]) - 1] + 1;
+  }
+}
+
+void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
+                const uint32_t* rflags) {
+  nout = 0;
+  if (!share || (fl & kFlagBitmap)) {
+    load_requests(n, a, b, fl, rflags);
+    return;
+  }
+  if (cap_out && n > cap_out) throw Error(VOSS_ERR_INVALID_ARG, "batch exceeds the plan's capacity");
+  cut_ranges(n, a, b, rflags, atom_a, atom_b, atom_rf, host_spans);
   // A fixed-capacity plan takes the atoms only if they fit (narrow atoms may
   // be tuned to smaller segments than the requests they came from);
   // otherwise the batch runs unshared, which always fits.
@@ -354,14 +370,6 @@ void Plan::load(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl,
       load_requests(n, a, b, fl, rflags);
       return;
     }
-  }
-  host_spans.assign(n, ReqSpan{0, 0, 0, 0});
-  for (uint32_t i = 0; i < n; ++i) {
-    host_spans[i].rflags = rflags ? rflags[i] : kReqGaps;
-    if (b[i] <= a[i]) continue;
-    // every piece inside the request is covered, so its atoms are contiguous
-    host_spans[i].s = atom_of[at(a[i])];
-    host_spans[i].e = atom_of[at(b[i]) - 1] + 1;
   }
   load_requests((uint32_t)atom_a.size(), atom_a.data(), atom_b.data(), fl, atom_rf.data());
   host_apos.assign(nreq, 0);

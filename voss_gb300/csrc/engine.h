@@ -239,6 +239,13 @@ cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads
                          cudaStream_t stream);
 cudaError_t launch_bucket_fill(const FillParams& fp, uint32_t grid, cudaStream_t stream);
 uint32_t bucket_fill_ctas_per_sm();      // resident fill CTAs per SM (occupancy query, cached)
+// Cut a batch's ranges at every endpoint into the disjoint pieces some range
+// covers (ascending); a piece gets kReqGaps if a range over it asks for gaps
+// (rflags NULL: all do).  spans[i] = the pieces [s, e) that tile range i.
+void cut_ranges(uint32_t n, const uint64_t* a, const uint64_t* b, const uint32_t* rflags,
+                std::vector<uint64_t>& atom_a, std::vector<uint64_t>& atom_b,
+                std::vector<uint32_t>& atom_rf, std::vector<ReqSpan>& spans);
+
 cudaError_t launch_combine(const BatchHdr* hdr, const ReqSpan* spans, const uint32_t* apos,
                            const ReqResult* ares, ReqResult* out, uint32_t grid, cudaStream_t stream);
 cudaError_t launch_finalize(const ReqDesc* reqs, const BatchHdr* hdr, const SegRec* segs,

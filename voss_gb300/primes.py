@@ -9,7 +9,7 @@ from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass, field
-from typing import List, Sequence
+from typing import List, Optional, Sequence
 
 from . import _capi
 from ._capi import (VOSS_ERR_INVALID_ARG, VOSS_ERR_INVALID_N, VOSS_PROFILE_FULL,
@@ -373,6 +373,31 @@ def range_stats_batch(ranges: Sequence[tuple]) -> List[RangeStats]:
     out = (_capi.VossRangeStats * max(n, 1))()
     _capi._check(_capi._lib.voss_primes_range_stats_batch(n, A, B, out), _ERRMAP)
     return [RangeStats.from_c(out[i]) for i in range(n)]
+
+
+def cut_ranges(ranges: Sequence[tuple], gaps: Optional[Sequence[bool]] = None):
+    """How a batch shares work: the disjoint pieces that the ranges cut each
+    other into, and for each range the pieces [first, last) that tile it.
+    Returns (pieces, spans): pieces = [(a, b, gaps_scanned)], spans = [(first,
+    last)].  Runs on the host (no GPU)."""
+    n = len(ranges)
+    A = (ctypes.c_uint64 * max(n, 1))()
+    B = (ctypes.c_uint64 * max(n, 1))()
+    for i, (a, b) in enumerate(ranges):
+        _check_range(a, b)
+        A[i], B[i] = a, b
+    G = None
+    if gaps is not None:
+        G = (ctypes.c_uint32 * max(n, 1))(*[1 if g else 0 for g in gaps])
+    cap = max(2 * n, 1)
+    pa, pb = (ctypes.c_uint64 * cap)(), (ctypes.c_uint64 * cap)()
+    pg = (ctypes.c_uint32 * cap)()
+    first, last = (ctypes.c_uint32 * max(n, 1))(), (ctypes.c_uint32 * max(n, 1))()
+    count = ctypes.c_uint64()
+    _capi._check(_capi._lib.voss_gb300_cut_ranges(n, A, B, G, cap, pa, pb, pg, ctypes.byref(count),
+                                                  first, last), _ERRMAP)
+    pieces = [(pa[j], pb[j], bool(pg[j])) for j in range(count.value)]
+    return pieces, [(first[i], last[i]) for i in range(n)]
 
 
 def get_config() -> dict:
