@@ -243,6 +243,18 @@ def test_goldbach_golden_and_oracle(vg, golden, oracle_lib):
     assert list(vg.conjectures.iter_goldbach_upto(1000)) == []
 
 
+def test_goldbach_many_tiles_per_cta(vg, oracle_lib):
+    """3*10^8: thousands of 65536-n tiles, several per CTA, so state carried
+    from tile to tile (maximum, sum, histogram) is exercised."""
+    N = 3 * 10**8
+    mine = vg.conjectures.goldbach_minp(N)
+    orc = oracle_lib.goldbach_minp(N)
+    assert np.array_equal(mine["minp"], orc["minp"])
+    assert mine["max"] == orc["max"] and mine["sum"] == orc["sum"]
+    assert np.array_equal(mine["hist"], orc["hist"])
+    assert mine["counterexamples"] == 0
+
+
 @pytest.mark.slow
 def test_goldbach_1e9_checksums(vg, oracle_lib):
     mine = vg.conjectures.goldbach_minp(10**9, want_array=False)
