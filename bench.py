@@ -16,10 +16,13 @@ roofline: the sieve kernel against this GPU's measured shared-memory peak.
 cpu_baseline: the CPU oracle (oracle/, C + OpenMP, all host cores) on a
   bounded sample of the same workload.
 
-Under torchrun (N > 1) every rank sieves its own 10^12 integers
-([r*10^12, (r+1)*10^12), weak scaling); the ranks exchange nothing but the
-final few-KB accumulators.  --impl reference times the reference algorithm's
-CPU restatement (the oracle) on the host cores, rank 0 only.
+Under torchrun (N > 1) the ranks share the same [0, 10^12) (strong scaling):
+it is cut into segment-aligned chunks of about 10^9 integers dealt
+round-robin, so every rank holds the same mix of offsets; each rank runs its
+chunks as one batched launch, and the ranks exchange nothing but the final
+per-chunk accumulators, which rank 0 stitches into the whole range's result
+(the same as one GPU's).  --impl reference times the reference algorithm's CPU
+restatement (the oracle) on the host cores, rank 0 only.
 """
 from __future__ import annotations
 
@@ -39,6 +42,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "integers sieved/sec (count+gaps) at 1e12 range"
 UNIT = "int/s"
 WIDTH = 10**12
+CHUNK = 10**9            # integers per chunk when the range is dealt over ranks
 # Context(10^12) STANDARD (count + gaps), 62.3 s on an A100
 PUBLISHED_INT_PER_S = 10**12 / 62.3
 
@@ -143,7 +147,7 @@ def run_reference(args, rank, world):
     desc = "4 windows of 10^9 integers at offsets 0, 2.5e11, 5e11, 7.5e11 of [0, 1e12) per step"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": value / PUBLISHED_INT_PER_S,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": value / PUBLISHED_INT_PER_S,
             "dtype": "u32/u64 integer", "data": "synthetic (the range itself is the input)",
             "config": {"workload": "range [0,1e12) full statistics (count+gaps+Chebyshev)",
                        "sample": desc},
@@ -275,12 +279,12 @@ def run_ours(args, rank, world, local_rank):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     import voss_gb300 as vg
     from voss_gb300.plan import SievePlan, smem_peak
-    from voss_gb300.shard import gather_merge
+    from voss_gb300.shard import gather_merge_many, interleaved_chunks
 
-    a, b = rank * WIDTH, (rank + 1) * WIDTH
+    ranges = interleaved_chunks(0, WIDTH, CHUNK, world, rank) if world > 1 else [(0, WIDTH)]
     stream = torch.cuda.Stream()
     flush = torch.empty(512 * 2**20, dtype=torch.uint8, device="cuda")
-    plan = SievePlan([(a, b)])
+    plan = SievePlan(ranges)
     info = plan.info()
     for _ in range(args.warmup):
         time_plan(plan, stream, torch, 1, flush)
@@ -300,34 +304,45 @@ def run_ours(args, rank, world, local_rank):
         t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-    res = plan.results(stream.cuda_stream)[0]
-    merged = gather_merge(res) if dist else res
+    res = plan.results(stream.cuda_stream)
+    merged = gather_merge_many(res) if dist else res[0]
+
+    # e2e: the reference-facing API over [0, 10^12).  One GPU: Context
+    # creation over [1, 10^12 - 1], the first query (the whole sieve run,
+    # results copied to host memory), the remaining queries from the cache,
+    # free.  N GPUs: each rank's chunks through voss_primes_range_stats_batch
+    # (host arrays in and out), slowest rank.
+    e2e_s, n_large = [], 0
+    for _ in range(max(1, min(args.steps, 3))):
+        barrier()
+        t0 = time.perf_counter()
+        if dist:
+            vg.range_stats_batch(ranges)
+        else:
+            with vg.Context(WIDTH - 1) as ctx:
+                ctx.statistics()
+                ctx.chebyshev()
+                ctx.twins()
+                n_large = len(ctx.large_gaps())
+        dt = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([dt], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        e2e_s.append(dt)
+    e2e_val = WIDTH / statistics.mean(e2e_s)
 
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
 
-    # e2e: the reference-facing API over [1, 10^12 - 1] = [0, 10^12): Context
-    # creation, the first query (the whole sieve run, results copied to host
-    # memory), the remaining queries from the cache, free.
-    e2e_s, n_large = [], 0
-    for _ in range(max(1, min(args.steps, 3))):
-        t0 = time.perf_counter()
-        with vg.Context(WIDTH - 1) as ctx:
-            ctx.statistics()
-            ctx.chebyshev()
-            ctx.twins()
-            n_large = len(ctx.large_gaps())
-        e2e_s.append(time.perf_counter() - t0)
-    e2e_val = WIDTH / statistics.mean(e2e_s)
-
     sieve_ms = statistics.mean(k[0] for k in kt)
     fin_ms = statistics.mean(k[1] for k in kt)
     peaks = smem_peak()
     alg_bytes = 8.0 * info["clears"] + 2.0 * info["wheel_bytes"]
     achieved = alg_bytes / (sieve_ms / 1e3) / 1e9
-    value = world * WIDTH / (total_ms / args.steps / 1e3)
+    value = WIDTH / (total_ms / args.steps / 1e3)
 
     cpu = None
     if not args.no_cpu:
@@ -342,15 +357,21 @@ def run_ours(args, rank, world, local_rank):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": value / PUBLISHED_INT_PER_S, "dtype": "u32/u64 integer",
+        "scaling": "strong", "vs_baseline": value / PUBLISHED_INT_PER_S, "dtype": "u32/u64 integer",
         "data": "synthetic (the range itself is the input)",
-        "config": {"workload": "range [0,1e12) full statistics (count+gaps+Chebyshev), per GPU",
+        "config": {"workload": "range [0,1e12) full statistics (count+gaps+Chebyshev)" +
+                   ("" if world == 1 else ", dealt over the ranks in %d chunks of about 1e9" %
+                    len(interleaved_chunks(0, WIDTH, CHUNK, 1, 0))),
                    "segments": info["segments"], "grid": info["grid"], "smem_bytes": info["smem_bytes"],
                    "l2": "flushed between steps (512 MB write outside the timed events)",
                    "parallelism": "dp%d" % world},
-        "e2e": {"value": e2e_val, "unit": UNIT, "api": "voss_primes_ctx_new/statistics/chebyshev/"
-                "twins/large_gaps/free (C ABI via ctypes)",
-                "h2d_bytes_per_step": 64, "d2h_bytes_per_step": 8 * (10 + 1025) + 4 + 16 * n_large},
+        "e2e": ({"value": e2e_val, "unit": UNIT, "api": "voss_primes_ctx_new/statistics/chebyshev/"
+                 "twins/large_gaps/free (C ABI via ctypes)",
+                 "h2d_bytes_per_step": 64, "d2h_bytes_per_step": 8 * (10 + 1025) + 4 + 16 * n_large}
+                if world == 1 else
+                {"value": e2e_val, "unit": UNIT, "api": "voss_primes_range_stats_batch per rank (C ABI via "
+                 "ctypes), slowest rank", "h2d_bytes_per_step": 24 + 88 * len(ranges),
+                 "d2h_bytes_per_step": 8280 * len(ranges)}),
         "gpu_launches": info["kernels_per_run"] * args.steps,
         "roofline": {"bound": "smem", "achieved": achieved, "peak": peaks["ldst_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["ldst_gbs"], "traffic": read_traffic(),

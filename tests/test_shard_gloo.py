@@ -79,3 +79,19 @@ def test_merge_many_pieces_matches_whole():
     cuts = [a, a + 1, a + 30, 999_500_000, 999_500_001, 1_000_000_007, 1_000_000_008, b]
     parts = [_stats_from_oracle(oracle.range_stats(x, y)) for x, y in zip(cuts, cuts[1:])]
     assert merge(parts) == _stats_from_oracle(oracle.range_stats(a, b))
+
+
+def test_interleaved_chunks_merge_to_whole():
+    """Chunks dealt round-robin over ranks cover the range once and merge
+    (from any rank order) to the whole range's result."""
+    import oracle
+    from voss_gb300.shard import ALIGN, interleaved_chunks, merge
+    oracle.build()
+    a, b, world = 12345, 3 * 10**8 + 7, 3
+    per_rank = [interleaved_chunks(a, b, 2 * 10**7, world, r) for r in range(world)]
+    allc = sorted(c for part in per_rank for c in part)
+    assert allc[0][0] == a and allc[-1][1] == b
+    assert all(x1 == y0 and x1 % ALIGN == 0 for (x0, x1), (y0, y1) in zip(allc, allc[1:]))
+    assert max(map(len, per_rank)) - min(map(len, per_rank)) <= 1
+    pieces = [_stats_from_oracle(oracle.range_stats(x, y, threads=4)) for part in reversed(per_rank) for x, y in part]
+    assert merge(sorted(pieces, key=lambda s: (s.a, s.b))) == _stats_from_oracle(oracle.range_stats(a, b))

@@ -35,6 +35,20 @@ def shard_ranges(a: int, b: int, world: int) -> List[tuple]:
     return [(cuts[i], cuts[i + 1]) for i in range(world)]
 
 
+def interleaved_chunks(a: int, b: int, chunk: int, world: int, rank: int) -> List[tuple]:
+    """Cut [a, b) at the multiples of a segment-aligned step near `chunk` and
+    deal the pieces round-robin: rank r gets pieces r, r + world, ...  Every
+    rank then holds the same mix of offsets, so ranks take about the same
+    time although the cost of an integer grows with its size."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("need 0 <= rank < world")
+    if b <= a:
+        return []
+    step = max(ALIGN, (chunk // ALIGN) * ALIGN)
+    cuts = [a] + list(range((a // step + 1) * step, b, step)) + [b]
+    return [(cuts[i], cuts[i + 1]) for i in range(rank, len(cuts) - 1, world)]
+
+
 def merge(parts: Sequence[RangeStats]) -> RangeStats:
     """Stitch results of consecutive ranges [a0,a1), [a1,a2), ... into [a0, an)."""
     parts = list(parts)
@@ -94,3 +108,13 @@ def gather_merge(local: RangeStats, group=None) -> RangeStats:
     objs: list = [None] * world
     dist.all_gather_object(objs, local, group=group)
     return merge(sorted(objs, key=lambda s: (s.a, s.b)))
+
+
+def gather_merge_many(local: Sequence[RangeStats], group=None) -> RangeStats:
+    """As gather_merge, for ranks that each hold several pieces (for example
+    interleaved chunks): all pieces of all ranks, merged in order."""
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    objs: list = [None] * world
+    dist.all_gather_object(objs, list(local), group=group)
+    return merge(sorted((x for part in objs for x in part), key=lambda s: (s.a, s.b)))
