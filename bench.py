@@ -17,7 +17,7 @@ cpu_baseline: the CPU oracle (oracle/, C + OpenMP, all host cores) on a
   bounded sample of the same workload.
 
 Under torchrun (N > 1) the ranks share the same [0, 10^12) (strong scaling):
-it is cut into segment-aligned chunks of about 10^9 integers dealt
+it is cut into segment-aligned chunks of about 2.5*10^8 integers dealt
 round-robin, so every rank holds the same mix of offsets; each rank runs its
 chunks as one batched launch, and the ranks exchange nothing but the final
 per-chunk accumulators, which rank 0 stitches into the whole range's result
@@ -42,7 +42,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "integers sieved/sec (count+gaps) at 1e12 range"
 UNIT = "int/s"
 WIDTH = 10**12
-CHUNK = 10**9            # integers per chunk when the range is dealt over ranks
+CHUNK = 25 * 10**7       # integers per chunk when the range is dealt over ranks
 # Context(10^12) STANDARD (count + gaps), 62.3 s on an A100
 PUBLISHED_INT_PER_S = 10**12 / 62.3
 
@@ -360,7 +360,7 @@ def run_ours(args, rank, world, local_rank):
         "scaling": "strong", "vs_baseline": value / PUBLISHED_INT_PER_S, "dtype": "u32/u64 integer",
         "data": "synthetic (the range itself is the input)",
         "config": {"workload": "range [0,1e12) full statistics (count+gaps+Chebyshev)" +
-                   ("" if world == 1 else ", dealt over the ranks in %d chunks of about 1e9" %
+                   ("" if world == 1 else ", dealt over the ranks in %d chunks of about 2.5e8" %
                     len(interleaved_chunks(0, WIDTH, CHUNK, 1, 0))),
                    "segments": info["segments"], "grid": info["grid"], "smem_bytes": info["smem_bytes"],
                    "l2": "flushed between steps (512 MB write outside the timed events)",
