@@ -387,26 +387,55 @@ sieve_segments_kernel(const SieveParams prm) {
       const uint32_t wend = min(wbeg + run, nwords);
       uint32_t first1 = 0, last1 = 0, cnt = 0, c41 = 0, c31 = 0, maxg = 0, maxgs = 0;
       const bool gaps = (s_cur.rflags & kReqGaps) != 0;
-      for (uint32_t wi = wbeg; wi < wend; ++wi) {
-        uint32_t w = seg[wi];
-        if (!w) continue;
-        cnt += __popc(w);
-        c41 += __popc(w & m41);
-        c31 += __popc(w & 0x2B2B2B2Bu);
-        const uint32_t vb = 120u * wi;
-        if (!gaps) {                        // counts only: keep first and last
+      if (gaps) {
+        // the run's first prime opens no gap: it is taken before the main
+        // loop, which then records a gap for every prime it meets
+        uint32_t wi = wbeg, pv = 0;
+        bool have = false;
+        for (; wi < wend && !have; ++wi) {
+          uint32_t w = seg[wi];
+          if (!w) continue;
+          cnt += __popc(w);
+          c41 += __popc(w & m41);
+          c31 += __popc(w & 0x2B2B2B2Bu);
+          const uint32_t vb = 120u * wi;
+          pv = vb + s_vtab[__ffs(w) - 1];
+          w &= w - 1u;
+          first1 = pv + 1u;
+          have = true;
+          while (w) {
+            const uint32_t v = vb + s_vtab[__ffs(w) - 1];
+            w &= w - 1u;
+            record_gap(sk, pv, v, maxg, maxgs);
+            pv = v;
+          }
+        }
+        for (; wi < wend; ++wi) {
+          uint32_t w = seg[wi];
+          if (!w) continue;
+          cnt += __popc(w);
+          c41 += __popc(w & m41);
+          c31 += __popc(w & 0x2B2B2B2Bu);
+          const uint32_t vb = 120u * wi;
+          do {
+            const uint32_t v = vb + s_vtab[__ffs(w) - 1];
+            w &= w - 1u;
+            record_gap(sk, pv, v, maxg, maxgs);
+            pv = v;
+          } while (w);
+        }
+        last1 = have ? pv + 1u : 0u;
+      } else {
+        for (uint32_t wi = wbeg; wi < wend; ++wi) {
+          const uint32_t w = seg[wi];
+          if (!w) continue;
+          cnt += __popc(w);
+          c41 += __popc(w & m41);
+          c31 += __popc(w & 0x2B2B2B2Bu);
+          const uint32_t vb = 120u * wi;
           if (!first1) first1 = vb + s_vtab[__ffs(w) - 1] + 1u;
           last1 = vb + s_vtab[31 - __clz(w)] + 1u;
-          continue;
         }
-        do {
-          const uint32_t bp = (uint32_t)__ffs(w) - 1u;
-          w &= w - 1u;
-          const uint32_t v = vb + s_vtab[bp];
-          if (last1) record_gap(sk, last1 - 1u, v, maxg, maxgs);
-          else first1 = v + 1u;
-          last1 = v + 1u;
-        } while (w);
       }
       // lane stitching: previous lane's last prime (values grow with the lane)
       uint32_t sc = last1;
