@@ -258,6 +258,8 @@ BucketPlan Engine::bucket_plan(const Config& c, uint64_t b, uint32_t nprimes, ui
 // ---------------------------------------------------------------------------
 // Plan
 // ---------------------------------------------------------------------------
+static uint64_t round16(uint64_t bytes) { return (bytes + 15) & ~uint64_t(15); }
+
 void Plan::reserve_capacity(uint32_t max_req, uint64_t max_segs, uint64_t max_bucket_entries) {
   cap_req = std::max<uint32_t>(max_req, 1);
   cap_segs = std::max<uint64_t>(max_segs, 1);
@@ -273,8 +275,9 @@ void Plan::reserve_capacity(uint32_t max_req, uint64_t max_segs, uint64_t max_bu
   cap_fill = max_bucket_entries ? 65536u : 0u;
   if (cap_bucket) bucket.reserve(4 * cap_bucket);
   if (cap_fill) fills.reserve(sizeof(FillItem) * cap_fill);
-  bcount.reserve(4 * cap_segs);
-  reqs.reserve(sizeof(ReqDesc) * cap_req);
+  bcount.reserve(round16(4 * cap_segs));
+  hdr.reserve(sizeof(BatchHdr) + sizeof(ReqDesc) * cap_req);
+  ctl.reserve(sizeof(PlanCtl));
   segs.reserve(sizeof(SegRec) * cap_segs);
   acc.reserve(sizeof(ReqAccum) * cap_req);
   results.reserve(sizeof(ReqResult) * cap_req);
@@ -484,7 +487,7 @@ void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint3
     seg_max = E.cfg.seg_bytes;     // fixed for graph replay
   } else {
     seg_max = std::max<uint32_t>(smax, 128);
-    reqs.reserve(sizeof(ReqDesc) * std::max<uint32_t>(n, 1));
+    hdr.reserve(sizeof(BatchHdr) + sizeof(ReqDesc) * std::max<uint32_t>(n, 1));
     segs.reserve(sizeof(SegRec) * std::max<uint64_t>(total_segs, 1));
     acc.reserve(sizeof(ReqAccum) * std::max<uint32_t>(n, 1));
     results.reserve(sizeof(ReqResult) * std::max<uint32_t>(n, 1));
@@ -499,13 +502,10 @@ void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint3
   if (!cap_req) {
     bucket.reserve(4 * std::max<uint64_t>(bucket_entries, 1));
     fills.reserve(sizeof(FillItem) * std::max<uint32_t>(nfill, 1));
-    bcount.reserve(4 * std::max<uint64_t>(total_segs, 1));
+    bcount.reserve(round16(4 * std::max<uint64_t>(total_segs, 1)));
   }
-  overflow.reserve(sizeof(unsigned int));
-  hdr.reserve(sizeof(BatchHdr));
-  queue.reserve(sizeof(unsigned long long));
+  ctl.reserve(sizeof(PlanCtl));
   large.reserve(sizeof(LargeGapRec) * large_cap);
-  nlarge.reserve(sizeof(unsigned int));
   BatchHdr* h = static_cast<BatchHdr*>(stage.ptr);
   h->total_segs = total_segs;
   h->nreq = nreq;
@@ -516,9 +516,9 @@ void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint3
   const uint64_t gcap = (uint64_t)E.sm_count * E.cfg.ctas_per_sm;
   grid = (uint32_t)(cap_req ? gcap : std::min<uint64_t>(total_segs, gcap));
 
-  prm.reqs = reqs.as<ReqDesc>();
+  prm.reqs = dreqs();
   prm.hdr = hdr.as<BatchHdr>();
-  prm.queue = queue.as<unsigned long long>();
+  prm.queue = &dctl()->queue;
   prm.P = E.dP.as<uint32_t>();
   prm.M = E.dM.as<uint64_t>();
   prm.R = E.dR.as<uint32_t>();
@@ -528,7 +528,7 @@ void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint3
   prm.segs = segs.as<SegRec>();
   prm.acc = acc.as<ReqAccum>();
   prm.large = large.as<LargeGapRec>();
-  prm.n_large = nlarge.as<unsigned int>();
+  prm.n_large = &dctl()->nlarge;
   prm.large_cap = large_cap;
   prm.flags = flags;
   prm.bitmap = bitmap.as<uint32_t>();
@@ -542,12 +542,8 @@ void Plan::prepare(uint32_t n, const uint64_t* a, const uint64_t* b, uint32_t fl
 
 void Plan::upload(cudaStream_t s) {
   const size_t bytes = sizeof(BatchHdr) + sizeof(ReqDesc) * nreq;
-  check_cuda(cudaMemcpyAsync(hdr.ptr, stage.ptr, sizeof(BatchHdr), cudaMemcpyHostToDevice, s),
-             "upload batch header");
-  if (nreq)
-    check_cuda(cudaMemcpyAsync(reqs.ptr, static_cast<const char*>(stage.ptr) + sizeof(BatchHdr),
-                               bytes - sizeof(BatchHdr), cudaMemcpyHostToDevice, s),
-               "upload requests");
+  check_cuda(cudaMemcpyAsync(hdr.ptr, stage.ptr, bytes, cudaMemcpyHostToDevice, s),
+             "upload batch header and requests");
   if (nfill)
     check_cuda(cudaMemcpyAsync(fills.ptr, host_fills.data(), sizeof(FillItem) * nfill,
                                cudaMemcpyHostToDevice, s), "upload fill items");
@@ -602,18 +598,17 @@ void Plan::run_device(cudaStream_t s) {
     if (!e) check_cuda(cudaEventCreate(&e), "cudaEventCreate");
   const uint32_t nacc = cap_req ? cap_req : nreq;
   if (nacc == 0) return;
-  check_cuda(cudaMemsetAsync(acc.ptr, 0, sizeof(ReqAccum) * nacc, s), "memset accumulators");
-  check_cuda(cudaMemsetAsync(nlarge.ptr, 0, sizeof(unsigned int), s), "memset large count");
-  check_cuda(cudaMemsetAsync(queue.ptr, 0, sizeof(unsigned long long), s), "memset work queue");
-  check_cuda(cudaMemsetAsync(overflow.ptr, 0, sizeof(unsigned int), s), "memset overflow");
+  // accumulators, control words and bucket counts: one zeroing launch
   const uint64_t nsegs_dev = cap_req ? cap_segs : total_segs;
-  if (nsegs_dev)
-    check_cuda(cudaMemsetAsync(bcount.ptr, 0, 4 * nsegs_dev, s), "memset bucket counts");
+  check_cuda(launch_zero(ZeroSpan{acc.ptr, sizeof(ReqAccum) * nacc / 16},
+                         ZeroSpan{ctl.ptr, sizeof(PlanCtl) / 16},
+                         ZeroSpan{bcount.ptr, round16(4 * nsegs_dev) / 16}, eng->sm_count * 4, s),
+             "zero_kernel");
   // the sieve's timed span covers the bucket fill that feeds it
   check_cuda(cudaEventRecord(ev[0], s), "event");
   if (cap_req ? cap_fill : nfill) {
     FillParams fp;
-    fp.reqs = reqs.as<ReqDesc>();
+    fp.reqs = dreqs();
     fp.hdr = hdr.as<BatchHdr>();
     fp.items = fills.as<FillItem>();
     fp.P = prm.P;
@@ -621,15 +616,15 @@ void Plan::run_device(cudaStream_t s) {
     fp.R = prm.R;
     fp.bucket = bucket.as<uint32_t>();
     fp.bcount = bcount.as<uint32_t>();
-    fp.overflow = overflow.as<unsigned int>();
+    fp.overflow = &dctl()->overflow;
     const uint32_t fgrid = cap_req ? fill_grid_max() : std::min<uint32_t>(nfill, fill_grid_max());
     check_cuda(launch_bucket_fill(fp, fgrid, s), "bucket_fill_kernel");
   }
   check_cuda(launch_sieve(prm, grid, threads, s), "sieve_segments_kernel");
   check_cuda(cudaEventRecord(ev[1], s), "event");
-  check_cuda(launch_finalize(reqs.as<ReqDesc>(), hdr.as<BatchHdr>(), segs.as<SegRec>(),
+  check_cuda(launch_finalize(dreqs(), hdr.as<BatchHdr>(), segs.as<SegRec>(),
                              acc.as<ReqAccum>(), large.as<LargeGapRec>(),
-                             nlarge.as<unsigned int>(), large_cap, results.as<ReqResult>(), nacc, s),
+                             &dctl()->nlarge, large_cap, results.as<ReqResult>(), nacc, s),
              "finalize_kernel");
   if (cap_req ? cap_out : nout)
     check_cuda(launch_combine(hdr.as<BatchHdr>(), spans.as<ReqSpan>(), apos.as<uint32_t>(),
@@ -647,7 +642,7 @@ void Plan::fetch_async(cudaStream_t s) {
                                cudaMemcpyDeviceToHost, s), "download results");
   if (nfill) {
     host_flag.reserve(sizeof(unsigned int));
-    check_cuda(cudaMemcpyAsync(host_flag.ptr, overflow.ptr, sizeof(unsigned int),
+    check_cuda(cudaMemcpyAsync(host_flag.ptr, &dctl()->overflow, sizeof(unsigned int),
                                cudaMemcpyDeviceToHost, s), "download overflow flag");
   }
 }
@@ -671,7 +666,7 @@ const ReqResult* Plan::fetch(cudaStream_t s) {
 
 std::vector<LargeGapRec> Plan::fetch_large(cudaStream_t s) {
   unsigned int n = 0;
-  check_cuda(cudaMemcpyAsync(&n, nlarge.ptr, sizeof(n), cudaMemcpyDeviceToHost, s), "large count");
+  check_cuda(cudaMemcpyAsync(&n, &dctl()->nlarge, sizeof(n), cudaMemcpyDeviceToHost, s), "large count");
   check_cuda(cudaStreamSynchronize(s), "large count");
   if (n > large_cap)
     throw Error(VOSS_ERR_INTERNAL, "large-gap buffer overflow (" + std::to_string(n) + " gaps)");

@@ -84,8 +84,12 @@ struct Plan {
   bool batch_mode = false;      // tune for throughput of many ranges
   std::vector<ReqDesc> host_reqs;   // device order
   std::vector<uint32_t> order;      // host_reqs[i] is the caller's request order[i]
-  DevBuf reqs, hdr, queue, segs, acc, large, nlarge, results, bitmap;
-  DevBuf bucket, bcount, fills, overflow;   // bucket sieve lists, per-segment counts, fill items
+  DevBuf hdr;                   // BatchHdr followed by ReqDesc[] (one upload)
+  DevBuf ctl;                   // PlanCtl: work queue, large-gap count, overflow flag
+  DevBuf segs, acc, large, results, bitmap;
+  DevBuf bucket, bcount, fills;   // bucket sieve lists, per-segment counts, fill items
+  ReqDesc* dreqs() const { return reinterpret_cast<ReqDesc*>(static_cast<char*>(hdr.ptr) + sizeof(BatchHdr)); }
+  PlanCtl* dctl() const { return ctl.as<PlanCtl>(); }
   uint64_t bucket_entries = 0;  // entries reserved by the current batch
   uint64_t cap_bucket = 0;      // fixed arena (graph-replayed plans); 0 = exact
   uint32_t nfill = 0;
@@ -246,6 +250,7 @@ void cut_ranges(uint32_t n, const uint64_t* a, const uint64_t* b, const uint32_t
                 std::vector<uint64_t>& atom_a, std::vector<uint64_t>& atom_b,
                 std::vector<uint32_t>& atom_rf, std::vector<ReqSpan>& spans);
 
+cudaError_t launch_zero(ZeroSpan z0, ZeroSpan z1, ZeroSpan z2, uint32_t max_grid, cudaStream_t stream);
 cudaError_t launch_combine(const BatchHdr* hdr, const ReqSpan* spans, const uint32_t* apos,
                            const ReqResult* ares, ReqResult* out, uint32_t grid, cudaStream_t stream);
 cudaError_t launch_finalize(const ReqDesc* reqs, const BatchHdr* hdr, const SegRec* segs,

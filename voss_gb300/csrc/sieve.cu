@@ -26,6 +26,8 @@
 // finalize_kernel (the reference does this on the host, context.cu:462-524);
 // combine_kernel rebuilds requests that shared atoms of a batch.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <cstdint>
 
 #include "sieve.cuh"
@@ -770,6 +772,17 @@ combine_kernel(const BatchHdr* __restrict__ hdr, const ReqSpan* __restrict__ spa
   }
 }
 
+// Zero up to three regions in one launch (a plan's accumulators, control
+// words and bucket counts, before each run).
+__global__ void zero_kernel(ZeroSpan z0, ZeroSpan z1, ZeroSpan z2) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+  for (uint64_t i = t0; i < z0.n16; i += stride) static_cast<uint4*>(z0.p)[i] = zero;
+  for (uint64_t i = t0; i < z1.n16; i += stride) static_cast<uint4*>(z1.p)[i] = zero;
+  for (uint64_t i = t0; i < z2.n16; i += stride) static_cast<uint4*>(z2.p)[i] = zero;
+}
+
 // ---------------------------------------------------------------------------
 // host-side launchers (called by the engine)
 // ---------------------------------------------------------------------------
@@ -797,6 +810,14 @@ cudaError_t launch_combine(const BatchHdr* hdr, const ReqSpan* spans, const uint
                            const ReqResult* ares, ReqResult* out, uint32_t grid, cudaStream_t stream) {
   if (grid == 0) return cudaSuccess;
   combine_kernel<<<grid, 256, 0, stream>>>(hdr, spans, apos, ares, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zero(ZeroSpan z0, ZeroSpan z1, ZeroSpan z2, uint32_t max_grid, cudaStream_t stream) {
+  const uint64_t n = std::max(z0.n16, std::max(z1.n16, z2.n16));
+  if (n == 0) return cudaSuccess;
+  const uint32_t grid = (uint32_t)std::min<uint64_t>((n + 255) / 256, max_grid);
+  zero_kernel<<<grid, 256, 0, stream>>>(z0, z1, z2);
   return cudaGetLastError();
 }
 

@@ -68,6 +68,19 @@ struct BatchHdr {
   uint32_t pad;
 };
 
+// Per-launch control words, zeroed together before each run.
+struct PlanCtl {
+  unsigned long long queue;   // work-queue head: next (request, segment) item
+  unsigned int nlarge;        // large gaps recorded
+  unsigned int overflow;      // a bucket list ran out of room
+};
+
+// A region to zero, in 16-byte units.
+struct ZeroSpan {
+  void* p;
+  uint64_t n16;
+};
+
 // A caller request served from shared atoms: its atoms are [s, e) in
 // position order.
 struct ReqSpan {

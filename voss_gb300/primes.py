@@ -305,6 +305,14 @@ def prev_prime(x: int) -> int:
 # ---------------------------------------------------------------------------
 # additive: statistics of arbitrary half-open ranges
 # ---------------------------------------------------------------------------
+_SCALAR_FIELDS = tuple(n for n, _ in _capi.VossRangeStats._fields_ if n != "gap_hist")
+
+
+def _u64_list(arr) -> list:
+    """A ctypes uint64 array as a list of Python ints."""
+    return memoryview(arr).cast("B").cast("Q").tolist()
+
+
 @dataclass
 class RangeStats:
     """Statistics of the primes q with a <= q < b (see voss_gb300.h)."""
@@ -329,9 +337,11 @@ class RangeStats:
 
     @classmethod
     def from_c(cls, s: "_capi.VossRangeStats", full=None) -> "RangeStats":
-        kw = {n: int(getattr(s, n)) for n, _ in _capi.VossRangeStats._fields_ if n != "gap_hist"}
-        return cls(gap_hist=[int(x) for x in s.gap_hist],
-                   gap_hist_full=[int(x) for x in full] if full is not None else [], **kw)
+        # c_uint64 fields read as Python ints; arrays through a memoryview
+        # (an element-wise walk of a ctypes array costs tens of microseconds)
+        kw = {n: getattr(s, n) for n in _SCALAR_FIELDS}
+        return cls(gap_hist=_u64_list(s.gap_hist),
+                   gap_hist_full=_u64_list(full) if full is not None else [], **kw)
 
     def gap_counts(self) -> dict:
         """{gap: count} from the full histogram (needs full=True)."""
