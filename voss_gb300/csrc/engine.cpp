@@ -113,6 +113,7 @@ void Engine::init() {
   build_tiles();
   scratch.eng = this;
   scratch.device = device;
+  scratch.timed = false;           // the one-call path reads no kernel times
   // the offset-regime table measured by voss_gb300/autotune.py on GB300
   static const TuneEntry kBuiltin[] = {
 #include "tune_table.inc"
@@ -605,7 +606,7 @@ void Plan::run_device(cudaStream_t s) {
                          ZeroSpan{bcount.ptr, round16(4 * nsegs_dev) / 16}, eng->sm_count * 4, s),
              "zero_kernel");
   // the sieve's timed span covers the bucket fill that feeds it
-  check_cuda(cudaEventRecord(ev[0], s), "event");
+  if (timed) check_cuda(cudaEventRecord(ev[0], s), "event");
   if (cap_req ? cap_fill : nfill) {
     FillParams fp;
     fp.reqs = dreqs();
@@ -621,7 +622,7 @@ void Plan::run_device(cudaStream_t s) {
     check_cuda(launch_bucket_fill(fp, fgrid, s), "bucket_fill_kernel");
   }
   check_cuda(launch_sieve(prm, grid, threads, s), "sieve_segments_kernel");
-  check_cuda(cudaEventRecord(ev[1], s), "event");
+  if (timed) check_cuda(cudaEventRecord(ev[1], s), "event");
   check_cuda(launch_finalize(dreqs(), hdr.as<BatchHdr>(), segs.as<SegRec>(),
                              acc.as<ReqAccum>(), large.as<LargeGapRec>(),
                              &dctl()->nlarge, large_cap, results.as<ReqResult>(), nacc, s),
@@ -630,7 +631,7 @@ void Plan::run_device(cudaStream_t s) {
     check_cuda(launch_combine(hdr.as<BatchHdr>(), spans.as<ReqSpan>(), apos.as<uint32_t>(),
                               results.as<ReqResult>(), rres.as<ReqResult>(), cap_req ? cap_out : nout, s),
                "combine_kernel");
-  check_cuda(cudaEventRecord(ev[2], s), "event");
+  if (timed) check_cuda(cudaEventRecord(ev[2], s), "event");
 }
 
 void Plan::fetch_async(cudaStream_t s) {

@@ -116,6 +116,7 @@ struct Plan {
   uint32_t flags = 0;
   SieveParams prm{};
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // before sieve, after sieve, after finalize
+  bool timed = true;            // record ev[] on each run (for kernel_ms)
 
   ~Plan();
   Plan() = default;

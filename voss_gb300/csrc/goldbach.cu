@@ -334,6 +334,7 @@ GoldbachPlan* goldbach_plan_create(Engine& E, uint64_t N) {
     per_sm = 1;
   g->grid = (uint32_t)std::min<uint64_t>(g->ntiles, (uint64_t)E.sm_count * per_sm);
   g->sieve.eng = &E;
+  g->sieve.timed = false;
   return g.release();
 }
 
