@@ -123,8 +123,9 @@ struct Plan {
   Plan(const Plan&) = delete;
   Plan& operator=(const Plan&) = delete;
 
-  // Kernels per run (sieve + finalize).
-  static constexpr uint32_t kKernels = 2;
+  // Kernels per run (zeroing + sieve + finalize; the bucket fill comes on top
+  // when the run has lists, combine when it shares atoms).
+  static constexpr uint32_t kKernels = 3;
 
   // Fix the capacity (requests, segments, bucket entries) of a
   // graph-replayed plan.  With share set, max_req and max_segs are the
