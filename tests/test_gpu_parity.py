@@ -175,6 +175,24 @@ def test_large_gaps_and_boundaries(vg, oracle_lib):
     assert st.max_gap == 540 and st.max_gap_start == 738832928467 - 540
 
 
+def test_context_1e12_reference_values(vg):
+    """pi(10^12) (BASELINE) and the reference's large-gap list to 10^12: 11
+    gaps >= 500, the largest 540 ending at 738 832 928 467
+    (test_primes.py:438-458)."""
+    with vg.Context(10**12) as ctx:
+        assert ctx.prime_count() == 37607912018
+        gaps = ctx.large_gaps()
+        assert len(gaps) == 11
+        assert (gaps[0].gap, gaps[0].position) == (540, 738832928467)
+        assert all(g.gap >= 500 for g in gaps)
+
+
+@pytest.mark.slow
+def test_prime_count_1e13(vg):
+    # pi(10^13) = 346 065 536 839, the reference's recorded value (STATE.md:103)
+    assert vg.primes.prime_count(10**13) == 346065536839
+
+
 def test_progress_callback_chunks(vg):
     seen = []
     with vg.Context(10**6) as ctx:
