@@ -56,7 +56,8 @@ int voss_primes_range_stats_ex(uint64_t a, uint64_t b, voss_range_stats_t* out,
  * sieve their common integers once: the ranges are cut at every endpoint
  * into disjoint pieces, each piece is sieved once and each range is rebuilt
  * from its pieces, gaps stitched where they meet; results are the same as
- * one call per range. */
+ * one call per range.  Batches of more than 32768 ranges run in chunks of
+ * that size (sharing within a chunk). */
 int voss_primes_range_stats_batch(uint64_t n, const uint64_t* a, const uint64_t* b,
                                   voss_range_stats_t* out);
 

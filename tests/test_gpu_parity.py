@@ -392,3 +392,19 @@ def test_batch_shares_overlapping_ranges(vg):
         for k in PUBLIC_KEYS:
             assert getattr(g, k) == getattr(alone, k), (a, b, k, getattr(g, k), getattr(alone, k))
     assert got[15].max_gap == 540 and got[18].max_gap == 540
+
+
+def test_batch_in_chunks(vg):
+    """More ranges than one launch takes: chunked, same answers as alone."""
+    rng = random.Random(77)
+    ranges = []
+    for _ in range(40000):
+        a = rng.randrange(0, 10**11)
+        ranges.append((a, a + rng.randrange(0, 20000)))
+    got = vg.range_stats_batch(ranges)
+    assert len(got) == len(ranges)
+    for i in list(range(0, 40000, 997)) + [32767, 32768, 39999]:
+        a, b = ranges[i]
+        alone = vg.range_stats(a, b)
+        for k in PUBLIC_KEYS:
+            assert getattr(got[i], k) == getattr(alone, k), (i, a, b, k)

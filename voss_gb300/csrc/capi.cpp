@@ -624,8 +624,14 @@ extern "C" int voss_primes_range_stats_batch(uint64_t n, const uint64_t* a, cons
   return guarded([&] {
     vg::Engine& E = vg::Engine::for_current_device();
     std::lock_guard<std::mutex> g(E.mu);
-    const vg::ReqResult* r = E.run((uint32_t)n, a, b, nullptr, true, true);
-    for (uint64_t i = 0; i < n; ++i) vg::to_public(r[i], a[i], b[i], out + i);
+    // chunks bound the device memory of one launch (about 16 KB per range
+    // with shared pieces); ranges share work within their chunk
+    constexpr uint64_t kChunk = 32768;
+    for (uint64_t i0 = 0; i0 < n; i0 += kChunk) {
+      const uint64_t m = std::min<uint64_t>(kChunk, n - i0);
+      const vg::ReqResult* r = E.run((uint32_t)m, a + i0, b + i0, nullptr, true, true);
+      for (uint64_t i = 0; i < m; ++i) vg::to_public(r[i], a[i0 + i], b[i0 + i], out + i0 + i);
+    }
     return VOSS_OK;
   }, VOSS_ERR_INTERNAL);
 }
