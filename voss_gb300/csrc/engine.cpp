@@ -170,6 +170,12 @@ void Engine::ensure_table(uint64_t pmax) {
     for (int o = 0; o < 8; ++o)
       R[8 * i + o] = (uint32_t)(((p - kW30[o] % p) % p) * inv30 % p);
   }
+  // The sieve kernel reads the first kConstPrimes entries from its own
+  // compile-time copy; the two must agree.
+  static constexpr ConstPrimeTable kConstTable = make_const_prime_table();
+  for (size_t i = 0; i < std::min<size_t>(n, kConstPrimes); ++i)
+    if (P[i] != kConstTable.p[i] || M[i] != kConstTable.m[i])
+      throw Error(VOSS_ERR_INTERNAL, "prime table differs from the kernel's constant table");
   // Plans launched earlier may still read the old table.
   check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize(table)");
   dP.reserve(std::max<size_t>(n, 1) * 4);

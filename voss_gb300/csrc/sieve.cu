@@ -9,8 +9,8 @@
 //   2. mark with shared-memory atomicAnd, in work units handed out heaviest
 //      first by a shared counter: primes 37 <= p < split one warp each
 //      (lane = residue class x stream, fixed bit mask per stream); split <=
-//      p < S four per warp-round (lane = prime x class); p >= S one lane
-//      each (at most one hit per class); primes from the request's bucket
+//      p < S four per warp-round (lane = prime x class); p >= S two per
+//      lane (at most one hit per class); primes from the request's bucket
 //      split on come from the segment's bucket list, 1024 entries per unit,
 //      read coalesced from HBM (filled by bucket_fill_kernel).  Each stream
 //      starts at max(p^2, segment low), as the reference's
@@ -37,6 +37,8 @@ namespace vg {
 __device__ __forceinline__ uint32_t w30(uint32_t o) {
   return (uint32_t)((kW30Packed >> (o << 3)) & 0xFFu);
 }
+
+__constant__ ConstPrimeTable cTab = make_const_prime_table();
 
 // x mod p by Barrett reduction with m = floor((2^64-1)/p).
 __device__ __forceinline__ uint32_t mod_barrett(uint64_t x, uint32_t p, uint64_t m) {
@@ -257,7 +259,7 @@ sieve_segments_kernel(const SieveParams prm) {
       const uint32_t nsmall = s_cur.split < np ? s_cur.split : np;
       const uint32_t hbeg = s_cur.huge < np ? max(s_cur.huge, nsmall) : np;
       const uint32_t nmidu = (hbeg - nsmall + 31u) / 32u;
-      const uint32_t nhugeu = (np - hbeg + 31u) / 32u;
+      const uint32_t nhugeu = (np - hbeg + 2u * kHugeHalf - 1u) / (2u * kHugeHalf);
       const uint32_t nscan = nsmall + nmidu + nhugeu;
       const uint32_t bcnt = s_cur.bcnt;
       const uint64_t bbase = s_cur.bbase;
@@ -270,8 +272,9 @@ sieve_segments_kernel(const SieveParams prm) {
         u = __shfl_sync(0xFFFFFFFFu, u, 0);
         if (u >= nunits) break;
         if (u < nsmall) {
-          const uint32_t p = __ldg(prm.P + u);
-          const uint32_t m = mod_barrett(k0, p, __ldg(prm.M + u));
+          const bool cst = u < kConstPrimes;
+          const uint32_t p = cst ? cTab.p[u] : __ldg(prm.P + u);
+          const uint32_t m = mod_barrett(k0, p, cst ? (uint64_t)cTab.m[u] : __ldg(prm.M + u));
           const uint32_t r = __ldg(prm.R + 8u * u + o);
           uint32_t s = r >= m ? r - m : r + p - m;
           if (30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
@@ -295,20 +298,30 @@ sieve_segments_kernel(const SieveParams prm) {
             clear_bit(seg, v & 0x3FFFFu, ~(1u << (v >> 18)));
           }
         } else if (u >= nsmall + nmidu) {
-          // huge tier: p >= S, at most one hit per class; a lane per prime,
-          // the eight classes unrolled, clears predicated (no loop).
-          const uint32_t i = hbeg + 32u * (u - nsmall - nmidu) + lane;
-          if (i < np) {
-            const uint32_t p = __ldg(prm.P + i);
-            const uint64_t mg = __ldg(prm.M + i);
-            uint32_t rr[8];
-            load_residues(prm.R, i, rr);
-            const uint32_t m = mod_barrett(k0, p, mg);
+          // huge tier: p >= S, at most one hit per class; 64-prime units, a
+          // lane per prime in each of two halves whose table loads are all
+          // issued first; the eight classes unrolled, clears predicated.
+          const uint32_t ib = hbeg + 2u * kHugeHalf * (u - nsmall - nmidu) + lane;
+          uint32_t pq[2], rq[2][8];
+          uint64_t mq[2];
+#pragma unroll
+          for (uint32_t q = 0; q < 2; ++q) {
+            // past the table end a lane repeats the last prime: its clears
+            // are the same bits again
+            const uint32_t i = min(ib + kHugeHalf * q, np - 1u);
+            pq[q] = __ldg(prm.P + i);
+            mq[q] = __ldg(prm.M + i);
+            load_residues(prm.R, i, rq[q]);
+          }
+#pragma unroll
+          for (uint32_t q = 0; q < 2; ++q) {
+            const uint32_t p = pq[q];
+            const uint32_t m = mod_barrett(k0, p, mq[q]);
             const uint64_t p2 = (uint64_t)p * p;
             const bool low = 30ull * k0 < p2;
 #pragma unroll
             for (uint32_t t = 0; t < 8; ++t) {
-              uint32_t s = rr[t] >= m ? rr[t] - m : rr[t] + p - m;
+              uint32_t s = rq[q][t] >= m ? rq[q][t] - m : rq[q][t] + p - m;
               // p >= the segment: s is the class's only candidate here, so
               // below p*p there is none (the next one is s + p)
               if (low && 30ull * (k0 + s) + w30(t) < p2) s = nbytes;

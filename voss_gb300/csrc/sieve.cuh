@@ -22,6 +22,26 @@ constexpr uint32_t kTileBPeriod = 19u * 23u * 29u * 31u;     // 392863 bytes
 constexpr uint32_t kFirstTablePrime = 37;   // smallest prime not in a tile
 constexpr int kMaxThreads = 1024;
 
+// The first kConstPrimes table primes (37, 41, 43, ...) with their Barrett
+// constants floor((2^64-1)/p), computed at compile time.  Every prime table
+// the sieve kernel is given starts with exactly these; the kernel reads them
+// from constant memory, where a warp-uniform index is a broadcast.
+constexpr uint32_t kConstPrimes = 1024;      // primes 37 .. 8243
+struct ConstPrimeTable {
+  uint32_t p[kConstPrimes];
+  unsigned long long m[kConstPrimes];
+};
+constexpr ConstPrimeTable make_const_prime_table() {
+  ConstPrimeTable t{};
+  uint32_t n = 0;
+  for (uint32_t c = kFirstTablePrime; n < kConstPrimes; c += 2) {
+    bool prime = true;
+    for (uint32_t d = 3; d * d <= c && prime; d += 2) prime = c % d != 0;
+    if (prime) { t.p[n] = c; t.m[n] = ~0ull / c; ++n; }
+  }
+  return t;
+}
+
 // Flags of one launch.
 constexpr uint32_t kFlagBitmap = 1u;     // also write the sieved words out
 
@@ -46,6 +66,7 @@ struct ReqDesc {
 constexpr uint32_t kReqGaps = 1u;
 constexpr uint32_t kMaxBucketSegs = 4096;    // segments of a bucket request (fill-kernel shared counts, 16-bit packing)
 constexpr uint32_t kBucketUnit = 1024;       // list entries per work unit of the sieve kernel
+constexpr uint32_t kHugeHalf = 32;           // primes per half of a huge-tier work unit (one per lane)
 constexpr uint32_t kFillPrimes = 256;        // bucket primes per fill work item
 constexpr uint32_t kFillHits = 16384;        // list entries per fill work item, about
 
