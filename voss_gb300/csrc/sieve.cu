@@ -115,9 +115,13 @@ __device__ __forceinline__ void record_gap(const GapSink& sk, uint32_t vprev, ui
 }
 
 // A claimed (request, segment) work item with what the CTA needs of it.
+// The edge masks fix the segment's first word, w = ((w & and0) | or0) &
+// keep0, and its last word, w &= keepl: the tile primes themselves (7..29
+// live in wheel byte 0, 31 in byte 1), 1, and the request's ends.
 struct SegItem {
-  uint64_t item, k0, seg_in_req, bbase;
+  uint64_t item, k0, bbase;
   uint32_t req, nbytes, np, split, huge, rflags, bcnt, valid;
+  uint32_t and0, or0, keep0, keepl;
 };
 
 // Number of leading i in [0, n) for which pred(i) holds (pred holds on a
@@ -174,8 +178,25 @@ __device__ __noinline__ void claim_item(unsigned long long* queue, const ReqDesc
       d.bbase = R.bucket_base + si * (uint64_t)R.bucket_cap;
     }
     d.item = item; d.valid = 1;
-    d.req = r; d.k0 = k0; d.seg_in_req = si; d.nbytes = nb; d.np = a;
+    d.req = r; d.k0 = k0; d.nbytes = nb; d.np = a;
     d.split = R.tier_split; d.huge = R.tier_huge; d.rflags = R.rflags;
+    uint32_t and0 = ~0u, or0 = 0u, keep0 = ~0u, keepl = ~0u;
+    if (k0 == 0) { and0 = 0xFFFFFE00u; or0 = 0x1FEu; }   // 1 no; 7..29, 31 yes
+    else if (k0 == 1) or0 = 1u;                            // 31
+    if (si == 0) {                                         // numbers below a
+      for (uint32_t o = 0; o < 8; ++o)
+        if (30ull * k0 + w30(o) < R.a) keep0 &= ~(1u << o);
+    }
+    if (k0 + nb == R.k_hi) {                               // numbers from b on
+      const uint32_t lb = nb - 1;
+      uint32_t m = 0;
+      for (uint32_t o = 0; o < 8; ++o)
+        if (30ull * (k0 + lb) + w30(o) >= R.b) m |= 1u << o;
+      keepl = ~(m << ((lb & 3u) << 3));
+      const uint32_t rem = nb & 3u;                        // bytes past the end
+      if (rem) keepl &= (1u << (rem << 3)) - 1u;
+    }
+    d.and0 = and0; d.or0 = or0; d.keep0 = keep0; d.keepl = keepl;
   }
 }
 
@@ -194,9 +215,10 @@ sieve_segments_kernel(const SieveParams prm) {
   uint32_t* shist = seg + (prm.seg_bytes >> 2);
   WarpRec* wrec = reinterpret_cast<WarpRec*>(shist + kSmemHistCopies * kSmemStride);
 
-  // the segment in hand, and the next one, claimed and looked up by thread 0
-  // while the others mark (so no thread waits on that lookup)
-  __shared__ SegItem s_cur, s_nxt;
+  // the segment in hand, s_item[cur], and the next one, s_item[cur ^ 1],
+  // claimed and looked up by warp 0 while the others mark (so no thread
+  // waits on that lookup)
+  __shared__ SegItem s_item[2];
   __shared__ uint32_t s_ctr;
   __shared__ uint32_t s_vtab[32];      // bit b of a word -> 30*(b/8) + W30[b%8]
 
@@ -210,22 +232,26 @@ sieve_segments_kernel(const SieveParams prm) {
 
   const uint64_t total_segs = prm.hdr->total_segs;
   const uint32_t nreq = prm.hdr->nreq;
-  if (warp == 0) claim_item(prm.queue, prm.reqs, prm.P, prm.bcount, total_segs, nreq, s_nxt, lane);
-  for (;;) {
+  uint32_t cur = 0;
+  if (warp == 0) claim_item(prm.queue, prm.reqs, prm.P, prm.bcount, total_segs, nreq, s_item[0], lane);
+  __syncthreads();
+  // Three barriers per segment: after the fill, after the marking, before
+  // the warps are stitched.  No thread reads the segment after the last one,
+  // so the next fill follows it directly.
+  for (;; cur ^= 1u) {
     // work queue: the next (request, segment) item, heaviest requests first
-    __syncthreads();
-    if (tid == 0) s_cur = s_nxt;
-    __syncthreads();
-    if (!s_cur.valid) break;
-    const uint64_t item = s_cur.item;
-    const uint32_t req = s_cur.req;
-    const uint64_t k0 = s_cur.k0;
-    const uint32_t nbytes = s_cur.nbytes;
+    const SegItem& S = s_item[cur];
+    if (!S.valid) break;
+    const uint64_t item = S.item;
+    const uint32_t req = S.req;
+    const uint64_t k0 = S.k0;
+    const uint32_t nbytes = S.nbytes;
     const uint32_t nwords = (nbytes + 3u) >> 2;
-    const uint32_t np = s_cur.np;
+    const uint32_t np = S.np;
 
     if ((int)req != cur_req) {
       if (cur_req >= 0) {                           // flush the previous request's bins
+        __syncthreads();                            // after warp 0's last stitching gaps
         for (uint32_t bn = tid; bn < (uint32_t)kSmemBins; bn += nthr) {
           uint32_t s = 0;
 #pragma unroll
@@ -256,14 +282,15 @@ sieve_segments_kernel(const SieveParams prm) {
     {
       // unit layout: [0, nsmall) small primes, then 32-prime units of the mid
       // tier (split <= p < S), then 32-prime units of the huge tier (p >= S)
-      const uint32_t nsmall = s_cur.split < np ? s_cur.split : np;
-      const uint32_t hbeg = s_cur.huge < np ? max(s_cur.huge, nsmall) : np;
+      const uint32_t nsmall = S.split < np ? S.split : np;
+      const uint32_t hbeg = S.huge < np ? max(S.huge, nsmall) : np;
       const uint32_t nmidu = (hbeg - nsmall + 31u) / 32u;
       const uint32_t nhugeu = (np - hbeg + 2u * kHugeHalf - 1u) / (2u * kHugeHalf);
       const uint32_t nscan = nsmall + nmidu + nhugeu;
-      const uint32_t bcnt = s_cur.bcnt;
-      const uint64_t bbase = s_cur.bbase;
-      if (warp == 0) claim_item(prm.queue, prm.reqs, prm.P, prm.bcount, total_segs, nreq, s_nxt, lane);   // overlaps the marking
+      const uint32_t bcnt = S.bcnt;
+      const uint64_t bbase = S.bbase;
+      if (warp == 0)                                // overlaps the marking
+        claim_item(prm.queue, prm.reqs, prm.P, prm.bcount, total_segs, nreq, s_item[cur ^ 1u], lane);
       const uint32_t nunits = nscan + (bcnt + kBucketUnit - 1) / kBucketUnit;
       const uint32_t o = lane & 7u, h = lane >> 3;
       for (;;) {
@@ -358,50 +385,31 @@ sieve_segments_kernel(const SieveParams prm) {
       }
     }
     __syncthreads();
-
-    // fix-ups: the tile primes themselves, 1, and the request's edges
-    if (tid == 0) {
-      const ReqDesc& R = prm.reqs[req];
-      // The tiles clear their own primes: 7..29 live in byte 0, 31 in byte 1.
-      if (k0 == 0) seg[0] = (seg[0] & 0xFFFFFE00u) | 0x1FEu;   // 1 no; 7..29, 31 yes
-      else if (k0 == 1) seg[0] |= 1u;                            // 31
-      if (s_cur.seg_in_req == 0) {
-        uint32_t m = 0;
-        for (uint32_t o = 0; o < 8; ++o) if (30ull * k0 + w30(o) < R.a) m |= 1u << o;
-        seg[0] &= ~m;
-      }
-      if (k0 + nbytes == R.k_hi) {
-        const uint32_t lb = nbytes - 1;
-        uint32_t m = 0;
-        for (uint32_t o = 0; o < 8; ++o) if (30ull * (k0 + lb) + w30(o) >= R.b) m |= 1u << o;
-        seg[lb >> 2] &= ~(m << ((lb & 3u) << 3));
-        const uint32_t rem = nbytes & 3u;
-        if (rem) seg[lb >> 2] &= (1u << (rem << 3)) - 1u;
-      }
-      s_ctr = 0;                                   // for the next segment's marking
-    }
-    __syncthreads();
-
-    if (prm.flags & kFlagBitmap) {
-      uint32_t* dst = prm.bitmap + ((k0 - prm.reqs[0].k_lo) >> 2);
-      for (uint32_t w = tid; w < nwords; w += nthr) dst[w] = seg[w];
-    }
+    if (tid == 0) s_ctr = 0;                        // every unit is taken: reset for the next segment
 
     // 3. reductions: each thread scans one contiguous run of words (odd
     //    length, so the lanes of a warp hit distinct banks); lanes are
-    //    stitched with a warp max-scan of their last prime, warps by thread 0.
+    //    stitched with a warp max-scan of their last prime, warps by warp 0.
     {
+      const uint32_t run = ((nwords + nthr - 1) / nthr) | 1u;
+      const uint32_t wbeg = min(tid * run, nwords);
+      const uint32_t wend = min(wbeg + run, nwords);
+      // edge fix-ups, each by the thread whose run holds the word
+      if (wbeg == 0 && wend > 0) seg[0] = ((seg[0] & S.and0) | S.or0) & S.keep0;
+      if (wbeg < wend && wend == nwords) seg[nwords - 1u] &= S.keepl;
+      if (prm.flags & kFlagBitmap) {
+        __syncthreads();
+        uint32_t* dst = prm.bitmap + ((k0 - prm.reqs[0].k_lo) >> 2);
+        for (uint32_t w = tid; w < nwords; w += nthr) dst[w] = seg[w];
+      }
       GapSink sk;
       sk.shist = shist + (warp % kSmemHistCopies) * kSmemStride;
       sk.acc = prm.acc + req;
       sk.large = prm.large; sk.n_large = prm.n_large; sk.cap = prm.large_cap;
       sk.req = req; sk.base = 30ull * k0;
       const uint32_t m41 = (k0 & 1ull) ? 0x99669966u : 0x66996699u;
-      const uint32_t run = ((nwords + nthr - 1) / nthr) | 1u;
-      const uint32_t wbeg = min(tid * run, nwords);
-      const uint32_t wend = min(wbeg + run, nwords);
       uint32_t first1 = 0, last1 = 0, cnt = 0, c41 = 0, c31 = 0, maxg = 0, maxgs = 0;
-      const bool gaps = (s_cur.rflags & kReqGaps) != 0;
+      const bool gaps = (S.rflags & kReqGaps) != 0;
       if (gaps) {
         // the run's first prime opens no gap: it is taken before the main
         // loop, which then records a gap for every prime it meets
@@ -477,29 +485,43 @@ sieve_segments_kernel(const SieveParams prm) {
         wrec[warp] = r;
       }
       __syncthreads();
-      if (tid == 0) {
-        uint32_t run1 = 0, fst1 = 0, tc = 0, t41 = 0, t31 = 0, bg = 0, bs = 0;
-        for (uint32_t wv = 0; wv < nwarps; ++wv) {
-          const WarpRec r = wrec[wv];
-          if (r.first1) {
-            if (!run1) fst1 = r.first1;
-            else if (gaps) record_gap(sk, run1 - 1u, r.first1 - 1u, bg, bs);
-            run1 = r.last1;
-          }
-          if (r.maxg > bg || (r.maxg == bg && r.maxg && r.maxgs < bs)) { bg = r.maxg; bs = r.maxgs; }
-          tc += r.cnt; t41 += r.c41; t31 += r.c31;
+      // warps are stitched like lanes, lane = warp: the gap from the last
+      // prime before a warp to its first prime, the largest gap (ties: the
+      // first), the sums
+      if (warp == 0) {
+        WarpRec r = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        if (lane < nwarps) r = wrec[lane];
+        uint32_t sw = r.last1;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, sw, d);
+          if ((int)lane >= d) sw = max(sw, t);
         }
-        SegRec sr;
-        sr.first = fst1 ? sk.base + fst1 - 1u : 0;
-        sr.last = run1 ? sk.base + run1 - 1u : 0;
-        sr.max_gap = bg;
-        sr.max_gap_start = bg ? sk.base + bs : 0;
-        sr.count = tc;
-        prm.segs[item] = sr;
-        if (tc) {
-          atomicAdd(&sk.acc->count, (unsigned long long)tc);
-          atomicAdd(&sk.acc->c41, (unsigned long long)t41);
-          atomicAdd(&sk.acc->c31, (unsigned long long)t31);
+        uint32_t before = __shfl_up_sync(0xFFFFFFFFu, sw, 1);
+        if (lane == 0) before = 0;
+        uint32_t bg = 0, bs = 0;
+        if (gaps && r.first1 && before) record_gap(sk, before - 1u, r.first1 - 1u, bg, bs);
+        if (r.maxg > bg) { bg = r.maxg; bs = r.maxgs; }   // on a tie the joining gap starts first
+        const uint32_t gm = __reduce_max_sync(0xFFFFFFFFu, bg);
+        const uint32_t gs = __reduce_min_sync(0xFFFFFFFFu, (bg == gm && gm) ? bs : 0xFFFFFFFFu);
+        const uint32_t fst1 = __reduce_min_sync(0xFFFFFFFFu, r.first1 ? r.first1 : 0xFFFFFFFFu);
+        const uint32_t run1 = __shfl_sync(0xFFFFFFFFu, sw, 31);
+        const uint32_t tc = __reduce_add_sync(0xFFFFFFFFu, r.cnt);
+        const uint32_t t41 = __reduce_add_sync(0xFFFFFFFFu, r.c41);
+        const uint32_t t31 = __reduce_add_sync(0xFFFFFFFFu, r.c31);
+        if (lane == 0) {
+          SegRec sr;
+          sr.first = fst1 != 0xFFFFFFFFu ? sk.base + fst1 - 1u : 0;
+          sr.last = run1 ? sk.base + run1 - 1u : 0;
+          sr.max_gap = gm;
+          sr.max_gap_start = gm ? sk.base + gs : 0;
+          sr.count = tc;
+          prm.segs[item] = sr;
+          if (tc) {
+            atomicAdd(&sk.acc->count, (unsigned long long)tc);
+            atomicAdd(&sk.acc->c41, (unsigned long long)t41);
+            atomicAdd(&sk.acc->c31, (unsigned long long)t31);
+          }
         }
       }
     }
