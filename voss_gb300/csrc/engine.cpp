@@ -124,27 +124,17 @@ void Engine::init() {
 }
 
 void Engine::build_tiles() {
-  auto make = [&](const uint32_t* ps, int nps, uint32_t period, DevBuf& dst) {
-    const size_t len = period + kMaxSegBytes + 64;
-    std::vector<uint8_t> t((len + 3) & ~size_t(3), 0);
-    for (uint32_t j = 0; j < period; ++j) {
-      uint8_t v = 0;
-      for (int o = 0; o < 8; ++o) {
-        const uint64_t x = 30ull * j + kW30[o];
-        bool comp = false;
-        for (int i = 0; i < nps; ++i) comp |= (x % ps[i]) == 0;
-        if (!comp) v |= (uint8_t)(1u << o);
-      }
-      t[j] = v;
-    }
-    for (size_t j = period; j < t.size(); ++j) t[j] = t[j - period];
+  auto make = [&](const uint32_t* ps, uint32_t period, DevBuf& dst) {
+    const uint32_t stride = tile_copy_stride(period, kMaxSegBytes);
+    std::vector<uint8_t> base(period), t((size_t)kTileShifts * stride);
+    build_tile_copies(ps, 4, period, stride, base.data(), t.data());
     dst.reserve(t.size());
     check_cuda(cudaMemcpy(dst.ptr, t.data(), t.size(), cudaMemcpyHostToDevice), "tile upload");
   };
   const uint32_t a[4] = {7, 11, 13, 17};
   const uint32_t b[4] = {19, 23, 29, 31};
-  make(a, 4, kTileAPeriod, tileA);
-  make(b, 4, kTileBPeriod, tileB);
+  make(a, kTileAPeriod, tileA);
+  make(b, kTileBPeriod, tileB);
 }
 
 void Engine::ensure_table(uint64_t pmax) {
@@ -531,6 +521,8 @@ void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint3
   prm.R = E.dR.as<uint32_t>();
   prm.tileA = E.tileA.as<uint32_t>();
   prm.tileB = E.tileB.as<uint32_t>();
+  prm.tile_a_stride16 = tile_copy_stride(kTileAPeriod, kMaxSegBytes) / 16;
+  prm.tile_b_stride16 = tile_copy_stride(kTileBPeriod, kMaxSegBytes) / 16;
   prm.seg_bytes = seg_max;
   prm.segs = segs.as<SegRec>();
   prm.acc = acc.as<ReqAccum>();

@@ -42,8 +42,10 @@ constexpr uint32_t kNaPrimeLimit = 1u << 20;        // sieving primes, p*p < 2^4
 constexpr uint32_t kNaPrimes = 82014;               // primes in [37, 2^20)
 constexpr uint32_t kNaStride = 82016;               // kNaPrimes rounded up to 32
 constexpr uint32_t kNaLargeCap = 4096;
-constexpr uint32_t kNaTileA = ((kTileAPeriod + kNaSegBytes + 64) + 3) & ~3u;
-constexpr uint32_t kNaTileB = ((kTileBPeriod + kNaSegBytes + 64) + 3) & ~3u;
+constexpr uint32_t kNaTileAStride = tile_copy_stride(kTileAPeriod, kNaSegBytes);
+constexpr uint32_t kNaTileBStride = tile_copy_stride(kTileBPeriod, kNaSegBytes);
+constexpr uint32_t kNaTileA = kTileShifts * kNaTileAStride;      // bytes of all copies
+constexpr uint32_t kNaTileB = kTileShifts * kNaTileBStride;
 
 struct NaScratch {
   BatchHdr hdr;
@@ -73,6 +75,7 @@ static uint64_t h_M[kNaStride];
 static uint32_t h_R[8 * kNaStride];
 static uint8_t h_tileA[kNaTileA];
 static uint8_t h_tileB[kNaTileB];
+static uint8_t h_tile_base[kTileBPeriod];      // one period of a tile, the larger of the two
 static uint8_t h_comp[kNaPrimeLimit];
 static bool h_built = false;
 
@@ -114,22 +117,9 @@ void build_host_tables() {
     for (int o = 0; o < 8; ++o) h_R[8 * n + o] = (uint32_t)(((p - kW30h[o] % p) % p) * inv30 % p);
     ++n;
   }
-  auto tile = [](uint8_t* t, uint32_t len, uint32_t period, const uint32_t* ps) {
-    for (uint32_t j = 0; j < period; ++j) {
-      uint8_t v = 0;
-      for (int o = 0; o < 8; ++o) {
-        const uint64_t x = 30ull * j + kW30h[o];
-        bool comp = false;
-        for (int i = 0; i < 4; ++i) comp |= (x % ps[i]) == 0;
-        if (!comp) v |= (uint8_t)(1u << o);
-      }
-      t[j] = v;
-    }
-    for (uint32_t j = period; j < len; ++j) t[j] = t[j - period];
-  };
   const uint32_t a[4] = {7, 11, 13, 17}, b[4] = {19, 23, 29, 31};
-  tile(h_tileA, kNaTileA, kTileAPeriod, a);
-  tile(h_tileB, kNaTileB, kTileBPeriod, b);
+  build_tile_copies(a, 4, kTileAPeriod, kNaTileAStride, h_tile_base, h_tileA);
+  build_tile_copies(b, 4, kTileBPeriod, kNaTileBStride, h_tile_base, h_tileB);
   h_built = (n == kNaPrimes);
 }
 
@@ -256,6 +246,8 @@ extern "C" int voss_primes_range_stats_noalloc(uint64_t a, uint64_t b, voss_rang
   prm.R = d.R;
   prm.tileA = d.tileA;
   prm.tileB = d.tileB;
+  prm.tile_a_stride16 = kNaTileAStride / 16;
+  prm.tile_b_stride16 = kNaTileBStride / 16;
   prm.seg_bytes = kNaSegBytes;
   prm.segs = sc->segs;
   prm.acc = &sc->acc;

@@ -4,7 +4,8 @@
 // shared memory, and takes (request, segment) items from a device work queue
 // (one global atomic per item; requests come heaviest first).  Per segment:
 //   1. fill: AND of two presieve tiles (primes 7..17 and 19..31) read at the
-//      segment's phase -- replaces the reference's memset + per-prime
+//      segment's phase, 16 bytes per load from the tile copy in which that
+//      phase is aligned -- replaces the reference's memset + per-prime
 //      launches for the smallest primes (context.cu:404-414);
 //   2. mark with shared-memory atomicAnd, in work units handed out heaviest
 //      first by a shared counter: primes 37 <= p < split one warp each
@@ -45,13 +46,6 @@ __device__ __forceinline__ uint32_t mod_barrett(uint64_t x, uint32_t p, uint64_t
   uint64_t q = __umul64hi(x, m);
   uint64_t r = x - q * (uint64_t)p;
   return (uint32_t)(r >= p ? r - p : r);
-}
-
-// 4 bytes of a tile starting at byte offset `off` (any alignment).
-__device__ __forceinline__ uint32_t tile_word(const uint32_t* __restrict__ t, uint32_t off) {
-  const uint32_t i = off >> 2;
-  const uint32_t lo = __ldg(t + i), hi = __ldg(t + i + 1);
-  return __funnelshift_r(lo, hi, (off & 3u) << 3);
 }
 
 // First hit (segment-local byte) of class o of prime p, moved up so that the
@@ -264,11 +258,18 @@ sieve_segments_kernel(const SieveParams prm) {
 
     // 1. presieve fill
     {
+      // copy (phase mod 16) of each tile holds the phase on a 16-byte boundary
       const uint32_t phA = (uint32_t)(k0 % kTileAPeriod);
       const uint32_t phB = (uint32_t)(k0 % kTileBPeriod);
+      const uint4* ta = reinterpret_cast<const uint4*>(prm.tileA) + (phA & 15u) * prm.tile_a_stride16 + (phA >> 4);
+      const uint4* tb = reinterpret_cast<const uint4*>(prm.tileB) + (phB & 15u) * prm.tile_b_stride16 + (phB >> 4);
+      uint4* seg4 = reinterpret_cast<uint4*>(seg);
+      const uint32_t n16 = (nbytes + 15u) >> 4;    // up to 3 words past the end: never read
 #pragma unroll 4
-      for (uint32_t w = tid; w < nwords; w += nthr)
-        seg[w] = tile_word(prm.tileA, phA + 4u * w) & tile_word(prm.tileB, phB + 4u * w);
+      for (uint32_t v = tid; v < n16; v += nthr) {
+        const uint4 x = __ldg(ta + v), y = __ldg(tb + v);
+        seg4[v] = make_uint4(x.x & y.x, x.y & y.y, x.z & y.z, x.w & y.w);
+      }
     }
     __syncthreads();
 

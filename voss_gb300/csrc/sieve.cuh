@@ -42,6 +42,44 @@ constexpr ConstPrimeTable make_const_prime_table() {
   return t;
 }
 
+// The presieve tiles are stored as kTileShifts copies, copy c starting c
+// bytes into the periodic pattern, so that the pattern at any byte phase
+// starts on a 16-byte boundary of one copy: the fill reads them with
+// aligned 16-byte loads.
+constexpr uint32_t kTileShifts = 16;
+
+// Bytes of one copy of a tile with the given period, for segments of up to
+// max_seg bytes (a multiple of 16).
+constexpr uint32_t tile_copy_stride(uint32_t period, uint32_t max_seg) {
+  return (period + max_seg + 32u + 15u) & ~15u;
+}
+
+// Host: the presieve tile of the primes ps (bit o of byte j set iff no p
+// divides 30j + W30[o]) as kTileShifts copies of `stride` bytes each, copy c
+// holding pattern bytes c, c+1, ...  base: scratch of `period` bytes; out:
+// kTileShifts * stride bytes.
+inline void build_tile_copies(const uint32_t* ps, int nps, uint32_t period, uint32_t stride,
+                              uint8_t* base, uint8_t* out) {
+  for (uint32_t j = 0; j < period; ++j) {
+    uint8_t v = 0;
+    for (uint32_t o = 0; o < 8; ++o) {
+      const uint64_t x = 30ull * j + ((kW30Packed >> (8u * o)) & 0xFFu);
+      bool comp = false;
+      for (int i = 0; i < nps; ++i) comp = comp || x % ps[i] == 0;
+      if (!comp) v = (uint8_t)(v | (1u << o));
+    }
+    base[j] = v;
+  }
+  for (uint32_t c = 0; c < kTileShifts; ++c) {
+    uint8_t* dst = out + (size_t)c * stride;
+    uint32_t j = c % period;
+    for (uint32_t x = 0; x < stride; ++x) {
+      dst[x] = base[j];
+      if (++j == period) j = 0;
+    }
+  }
+}
+
 // Flags of one launch.
 constexpr uint32_t kFlagBitmap = 1u;     // also write the sieved words out
 
@@ -148,8 +186,10 @@ struct SieveParams {
   const uint32_t* P;         // table primes >= 37, ascending
   const uint64_t* M;         // floor((2^64-1)/p), for x mod p
   const uint32_t* R;         // R[8 * i + o]: k = R (mod p) <=> p | 30k+W30[o] (32 B per prime)
-  const uint32_t* tileA;     // presieve tiles, extended past their period
+  const uint32_t* tileA;     // presieve tiles: kTileShifts shifted copies each
   const uint32_t* tileB;
+  uint32_t tile_a_stride16;  // 16-byte units per copy of tile A
+  uint32_t tile_b_stride16;
   uint32_t seg_bytes;        // the largest segment of the launch (shared memory)
   SegRec* segs;
   ReqAccum* acc;
