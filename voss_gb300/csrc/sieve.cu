@@ -62,9 +62,10 @@ __device__ __forceinline__ uint32_t lift_to_square(uint32_t s, uint64_t k0, uint
 }
 
 // Clear the candidate of byte j, class o, given keep = ~(1 << o): the mask
-// is keep rotated to byte j & 3 of its word.
+// is keep rotated to byte j & 3 of its word (a funnel shift uses its count
+// mod 32, so 8 * j rotates by 8 * (j & 3)).
 __device__ __forceinline__ void clear_bit(uint32_t* seg, uint32_t j, uint32_t keep) {
-  atomicAnd(seg + (j >> 2), __funnelshift_l(keep, keep, (j & 3u) << 3));
+  atomicAnd(seg + (j >> 2), __funnelshift_l(keep, keep, j << 3));
 }
 
 // The eight class residues of table prime i (32 bytes, two vector loads).
@@ -347,14 +348,21 @@ sieve_segments_kernel(const SieveParams prm) {
             const uint32_t m = mod_barrett(k0, p, mq[q]);
             const uint64_t p2 = (uint64_t)p * p;
             const bool low = 30ull * k0 < p2;
+            uint32_t sv[8];
 #pragma unroll
-            for (uint32_t t = 0; t < 8; ++t) {
-              uint32_t s = rq[q][t] >= m ? rq[q][t] - m : rq[q][t] + p - m;
-              // p >= the segment: s is the class's only candidate here, so
-              // below p*p there is none (the next one is s + p)
-              if (low && 30ull * (k0 + s) + w30(t) < p2) s = nbytes;
-              if (s < nbytes) clear_bit(seg, s, ~(1u << t));
+            for (uint32_t t = 0; t < 8; ++t) sv[t] = rq[q][t] >= m ? rq[q][t] - m : rq[q][t] + p - m;
+            // p >= the segment: sv[t] is the class's only candidate here, so
+            // below p*p there is none (the next one is sv[t] + p).  The test
+            // sits apart from the clears, under one branch taken by few
+            // segments.
+            if (low) {
+#pragma unroll
+              for (uint32_t t = 0; t < 8; ++t)
+                if (30ull * (k0 + sv[t]) + w30(t) < p2) sv[t] = nbytes;
             }
+#pragma unroll
+            for (uint32_t t = 0; t < 8; ++t)
+              if (sv[t] < nbytes) clear_bit(seg, sv[t], ~(1u << t));
           }
         } else {
           // mid tier: p and k0 mod p once per prime (lane = prime), then
