@@ -323,8 +323,10 @@ sieve_segments_kernel(const SieveParams prm) {
           const uint32_t lim = min(kBucketUnit, bcnt - (u - nscan) * kBucketUnit);
 #pragma unroll 8
           for (uint32_t e = lane; e < lim; e += 32) {
+            // entry = bit index: word v / 32, and ~(1 << (v mod 32)) is
+            // 0xFFFFFFFE rotated by v (a funnel shift takes its count mod 32)
             const uint32_t v = __ldg(prm.bucket + base + e);
-            clear_bit(seg, v & 0x3FFFFu, ~(1u << (v >> 18)));
+            atomicAnd(seg + (v >> 5), __funnelshift_l(0xFFFFFFFEu, 0xFFFFFFFEu, v));
           }
         } else if (u >= nsmall + nmidu) {
           // huge tier: p >= S, at most one hit per class; 64-prime units, a
@@ -711,10 +713,9 @@ bucket_fill_kernel(const FillParams fp) {
             if (off >= S) { off -= S; ++sg; }
           }
         } else {
-          const uint32_t tag = (uint32_t)o << 18;
           for (; k < hi; k += p) {
             const uint32_t pos = atomicAdd(&cnt[sg], 1u);
-            if (pos < cap) list[(size_t)sg * cap + pos] = tag | off;
+            if (pos < cap) list[(size_t)sg * cap + pos] = bucket_entry(off, (uint32_t)o);
             else atomicOr(fp.overflow, 1u);
             off += pr; sg += pq;
             if (off >= S) { off -= S; ++sg; }

@@ -108,8 +108,9 @@ constexpr uint32_t kHugeHalf = 32;           // primes per half of a huge-tier w
 constexpr uint32_t kFillPrimes = 256;        // bucket primes per fill work item
 constexpr uint32_t kFillHits = 16384;        // list entries per fill work item, about
 
-// A bucket list entry: the segment-local byte (< 2^18) and the class.
-__host__ __device__ constexpr uint32_t bucket_entry(uint32_t off, uint32_t o) { return off | (o << 18); }
+// A bucket list entry: the segment-local bit index 8 * byte + class, so that
+// entry / 32 is the word and entry mod 32 the bit within it.
+__host__ __device__ constexpr uint32_t bucket_entry(uint32_t off, uint32_t o) { return (off << 3) | o; }
 
 // One fill work item: the hits of bucket primes [p0, p1) (table indices) of
 // request req that fall in its segments [g0, g1), packed g0 | g1 << 16.
