@@ -29,6 +29,9 @@ thread_local std::string g_last_error;
 void set_err(const std::string& m) { g_last_error = m; }
 
 constexpr uint64_t kMaxN = 100000000000000ull;   // 10^14
+// The smallest accepted tier split.  Splits below the first table prime (61)
+// leave the warp-per-prime tier empty.
+constexpr uint32_t kMinTierSplit = 37;
 
 // Run f, converting exceptions to codes.  `compute_code` is the code the
 // reference returns for a failure inside the computation.
@@ -693,7 +696,7 @@ extern "C" int voss_gb300_set_config(const voss_gb300_config_t* c) {
     set_err("threads must be a multiple of 32 in [64, 1024]");
     return VOSS_ERR_INVALID_ARG;
   }
-  if (c->tier_split && c->tier_split < vg::kFirstTablePrime) {
+  if (c->tier_split && c->tier_split < kMinTierSplit) {
     set_err("tier_split must be >= 37");
     return VOSS_ERR_INVALID_ARG;
   }
@@ -720,7 +723,7 @@ extern "C" int voss_gb300_set_tuning(uint32_t n, const voss_gb300_tune_entry_t* 
   if (n && !e) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
   for (uint32_t i = 0; i < n; ++i)
     if (e[i].seg_bytes < 1024 || e[i].seg_bytes > 221184 || e[i].seg_bytes % 128 ||
-        e[i].tier_split < vg::kFirstTablePrime) {
+        e[i].tier_split < kMinTierSplit) {
       set_err("tuning entry out of range (seg_bytes in [1024, 221184], multiple of 128; tier_split >= 37)");
       return VOSS_ERR_INVALID_ARG;
     }

@@ -3,7 +3,7 @@
 // Replaces the reference's per-call host orchestration
 // (library/src/primes/context.cu:212-559, prime_count.cu:141-293,
 // range.cu:99-262).  Differences by design:
-//   * the sieving-prime table (primes >= 37, with Barrett constants and the
+//   * the sieving-prime table (primes >= 61, with Barrett constants and the
 //     eight residue-class starts of each prime) is built once per process and
 //     stays resident on the device, growing on demand up to sqrt(10^14+10^10);
 //   * a run is two kernel launches for any number of ranges and segments,
@@ -124,17 +124,16 @@ void Engine::init() {
 }
 
 void Engine::build_tiles() {
-  auto make = [&](const uint32_t* ps, uint32_t period, DevBuf& dst) {
+  std::vector<uint8_t> base(kMaxTilePeriod);
+  for (int t = 0; t < kTiles; ++t) {
+    const uint32_t period = tile_period(t);
     const uint32_t stride = tile_copy_stride(period, kMaxSegBytes);
-    std::vector<uint8_t> base(period), t((size_t)kTileShifts * stride);
-    build_tile_copies(ps, 4, period, stride, base.data(), t.data());
-    dst.reserve(t.size());
-    check_cuda(cudaMemcpy(dst.ptr, t.data(), t.size(), cudaMemcpyHostToDevice), "tile upload");
-  };
-  const uint32_t a[4] = {7, 11, 13, 17};
-  const uint32_t b[4] = {19, 23, 29, 31};
-  make(a, kTileAPeriod, tileA);
-  make(b, kTileBPeriod, tileB);
+    const int nps = kTilePrimes[t][3] ? 4 : 3;
+    std::vector<uint8_t> copies((size_t)kTileShifts * stride);
+    build_tile_copies(kTilePrimes[t], nps, period, stride, base.data(), copies.data());
+    tile[t].reserve(copies.size());
+    check_cuda(cudaMemcpy(tile[t].ptr, copies.data(), copies.size(), cudaMemcpyHostToDevice), "tile upload");
+  }
 }
 
 void Engine::ensure_table(uint64_t pmax) {
@@ -519,10 +518,10 @@ void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint3
   prm.P = E.dP.as<uint32_t>();
   prm.M = E.dM.as<uint64_t>();
   prm.R = E.dR.as<uint32_t>();
-  prm.tileA = E.tileA.as<uint32_t>();
-  prm.tileB = E.tileB.as<uint32_t>();
-  prm.tile_a_stride16 = tile_copy_stride(kTileAPeriod, kMaxSegBytes) / 16;
-  prm.tile_b_stride16 = tile_copy_stride(kTileBPeriod, kMaxSegBytes) / 16;
+  for (int t = 0; t < kTiles; ++t) {
+    prm.tile[t] = E.tile[t].as<uint32_t>();
+    prm.tile_stride16[t] = tile_copy_stride(tile_period(t), kMaxSegBytes) / 16;
+  }
   prm.seg_bytes = seg_max;
   prm.segs = segs.as<SegRec>();
   prm.acc = acc.as<ReqAccum>();
@@ -687,23 +686,26 @@ uint64_t Plan::wheel_bytes() const {
 }
 
 uint64_t Plan::algorithmic_clears() const {
-  // Exactly the clears the marking tiers perform: for each table prime p
-  // (>= 37, p*p < b) and class o, the k in [k_lo, k_hi) with
-  // k = R (mod p) and 30k + W30[o] >= p*p.
+  // The candidate clears of Eratosthenes by the primes p >= 37 with
+  // p*p < b: for each such p and class o, the k in [k_lo, k_hi) with
+  // k = R (mod p) and 30k + W30[o] >= p*p.  The table primes (>= 61) are
+  // cleared by the marking tiers, 37..59 by the presieve tiles; both count.
   const Engine& E = *eng;
   uint64_t total = 0;
-  for (const ReqDesc& r : host_reqs) {
-    for (uint32_t i = 0; i < r.nprimes; ++i) {
-      const uint64_t p = E.hP[i];
-      const int64_t inv30 = inverse_mod((int64_t)(30 % p), (int64_t)p);
-      for (int o = 0; o < 8; ++o) {
-        const uint64_t rr = ((p - kW30[o] % p) % p) * (uint64_t)inv30 % p;
-        uint64_t k = r.k_lo + (rr + p - r.k_lo % p) % p;
-        const uint64_t n = 30 * k + kW30[o];
-        if (n < p * p) k += ((p * p - n + 30 * p - 1) / (30 * p)) * p;
-        if (k < r.k_hi) total += (r.k_hi - 1 - k) / p + 1;
-      }
+  auto clears = [&](const ReqDesc& r, uint64_t p) {
+    const int64_t inv30 = inverse_mod((int64_t)(30 % p), (int64_t)p);
+    for (int o = 0; o < 8; ++o) {
+      const uint64_t rr = ((p - kW30[o] % p) % p) * (uint64_t)inv30 % p;
+      uint64_t k = r.k_lo + (rr + p - r.k_lo % p) % p;
+      const uint64_t n = 30 * k + kW30[o];
+      if (n < p * p) k += ((p * p - n + 30 * p - 1) / (30 * p)) * p;
+      if (k < r.k_hi) total += (r.k_hi - 1 - k) / p + 1;
     }
+  };
+  for (const ReqDesc& r : host_reqs) {
+    for (uint64_t p : {37ull, 41ull, 43ull, 47ull, 53ull, 59ull})
+      if (p * p < r.b) clears(r, p);
+    for (uint32_t i = 0; i < r.nprimes; ++i) clears(r, E.hP[i]);
   }
   return total;
 }

@@ -201,12 +201,12 @@ class Engine {
   cudaStream_t stream = nullptr;
   Config cfg;
 
-  // Resident sieving-prime table: primes >= 37 up to table_limit.
+  // Resident sieving-prime table: primes >= 61 up to table_limit.
   std::vector<uint32_t> hP;
   std::vector<double> hInvPrefix;   // sum of 1/p over table primes [0, i)
   uint64_t table_limit = 0;
   DevBuf dP, dM, dR;            // primes, Barrett constants, class residues (8 per prime)
-  DevBuf tileA, tileB;
+  DevBuf tile[kTiles];        // presieve tiles, kTileShifts shifted copies each
 
   // Scratch plan reused by the synchronous entry points.
   Plan scratch;

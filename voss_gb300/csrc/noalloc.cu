@@ -39,13 +39,15 @@ constexpr uint32_t kNaSegBytes = 221184;           // largest segment
 constexpr uint32_t kNaMaxSegs = 65536;
 constexpr uint64_t kNaMaxB = 1ull << 40;
 constexpr uint32_t kNaPrimeLimit = 1u << 20;        // sieving primes, p*p < 2^40
-constexpr uint32_t kNaPrimes = 82014;               // primes in [37, 2^20)
+constexpr uint32_t kNaPrimes = 82008;               // primes in [61, 2^20)
 constexpr uint32_t kNaStride = 82016;               // kNaPrimes rounded up to 32
 constexpr uint32_t kNaLargeCap = 4096;
-constexpr uint32_t kNaTileAStride = tile_copy_stride(kTileAPeriod, kNaSegBytes);
-constexpr uint32_t kNaTileBStride = tile_copy_stride(kTileBPeriod, kNaSegBytes);
-constexpr uint32_t kNaTileA = kTileShifts * kNaTileAStride;      // bytes of all copies
-constexpr uint32_t kNaTileB = kTileShifts * kNaTileBStride;
+// tile t: kTileShifts copies of kNaTileStride(t) bytes
+constexpr uint32_t kNaTileStride0 = tile_copy_stride(tile_period(0), kNaSegBytes);
+constexpr uint32_t kNaTileStride1 = tile_copy_stride(tile_period(1), kNaSegBytes);
+constexpr uint32_t kNaTileStride2 = tile_copy_stride(tile_period(2), kNaSegBytes);
+constexpr uint32_t kNaTileStride3 = tile_copy_stride(tile_period(3), kNaSegBytes);
+constexpr uint32_t kNaTileStride[kTiles] = {kNaTileStride0, kNaTileStride1, kNaTileStride2, kNaTileStride3};
 
 struct NaScratch {
   BatchHdr hdr;
@@ -66,23 +68,29 @@ static __device__ __align__(256) unsigned char g_na_scratch[sizeof(NaScratch)];
 static __device__ __align__(256) uint32_t g_na_P[kNaStride];
 static __device__ __align__(256) uint64_t g_na_M[kNaStride];
 static __device__ __align__(256) uint32_t g_na_R[8 * kNaStride];
-static __device__ __align__(256) uint32_t g_na_tileA[kNaTileA / 4];
-static __device__ __align__(256) uint32_t g_na_tileB[kNaTileB / 4];
+static __device__ __align__(256) uint32_t g_na_tile0[kTileShifts * kNaTileStride0 / 4];
+static __device__ __align__(256) uint32_t g_na_tile1[kTileShifts * kNaTileStride1 / 4];
+static __device__ __align__(256) uint32_t g_na_tile2[kTileShifts * kNaTileStride2 / 4];
+static __device__ __align__(256) uint32_t g_na_tile3[kTileShifts * kNaTileStride3 / 4];
 
 // Host copies of the tables, built once per process in static storage.
 static uint32_t h_P[kNaStride];
 static uint64_t h_M[kNaStride];
 static uint32_t h_R[8 * kNaStride];
-static uint8_t h_tileA[kNaTileA];
-static uint8_t h_tileB[kNaTileB];
-static uint8_t h_tile_base[kTileBPeriod];      // one period of a tile, the larger of the two
+static uint8_t h_tile0[kTileShifts * kNaTileStride0];
+static uint8_t h_tile1[kTileShifts * kNaTileStride1];
+static uint8_t h_tile2[kTileShifts * kNaTileStride2];
+static uint8_t h_tile3[kTileShifts * kNaTileStride3];
+static uint8_t* const h_tile[kTiles] = {h_tile0, h_tile1, h_tile2, h_tile3};
+static uint8_t h_tile_base[kMaxTilePeriod];    // one period of a tile
 static uint8_t h_comp[kNaPrimeLimit];
 static bool h_built = false;
 
 struct NaDevice {
   bool ready = false;
   NaScratch* scratch = nullptr;
-  uint32_t *P = nullptr, *R = nullptr, *tileA = nullptr, *tileB = nullptr;
+  uint32_t *P = nullptr, *R = nullptr;
+  uint32_t* tile[kTiles] = {};
   uint64_t* M = nullptr;
   uint32_t sms = 0;
 };
@@ -117,9 +125,9 @@ void build_host_tables() {
     for (int o = 0; o < 8; ++o) h_R[8 * n + o] = (uint32_t)(((p - kW30h[o] % p) % p) * inv30 % p);
     ++n;
   }
-  const uint32_t a[4] = {7, 11, 13, 17}, b[4] = {19, 23, 29, 31};
-  build_tile_copies(a, 4, kTileAPeriod, kNaTileAStride, h_tile_base, h_tileA);
-  build_tile_copies(b, 4, kTileBPeriod, kNaTileBStride, h_tile_base, h_tileB);
+  for (int t = 0; t < kTiles; ++t)
+    build_tile_copies(kTilePrimes[t], kTilePrimes[t][3] ? 4 : 3, tile_period(t), kNaTileStride[t], h_tile_base,
+                      h_tile[t]);
   h_built = (n == kNaPrimes);
 }
 
@@ -137,13 +145,16 @@ int setup(int dev) {
   if (!h_built) return VOSS_ERR_INTERNAL;
   if (symbol_ptr(&d.scratch, g_na_scratch) != cudaSuccess || symbol_ptr(&d.P, g_na_P) != cudaSuccess ||
       symbol_ptr(&d.M, g_na_M) != cudaSuccess || symbol_ptr(&d.R, g_na_R) != cudaSuccess ||
-      symbol_ptr(&d.tileA, g_na_tileA) != cudaSuccess || symbol_ptr(&d.tileB, g_na_tileB) != cudaSuccess)
+      symbol_ptr(&d.tile[0], g_na_tile0) != cudaSuccess || symbol_ptr(&d.tile[1], g_na_tile1) != cudaSuccess ||
+      symbol_ptr(&d.tile[2], g_na_tile2) != cudaSuccess || symbol_ptr(&d.tile[3], g_na_tile3) != cudaSuccess)
     return VOSS_ERR_CUDA;
   if (cudaMemcpyToSymbol(g_na_P, h_P, sizeof(h_P)) != cudaSuccess ||
       cudaMemcpyToSymbol(g_na_M, h_M, sizeof(h_M)) != cudaSuccess ||
       cudaMemcpyToSymbol(g_na_R, h_R, sizeof(h_R)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_na_tileA, h_tileA, sizeof(h_tileA)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_na_tileB, h_tileB, sizeof(h_tileB)) != cudaSuccess)
+      cudaMemcpyToSymbol(g_na_tile0, h_tile0, sizeof(h_tile0)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_na_tile1, h_tile1, sizeof(h_tile1)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_na_tile2, h_tile2, sizeof(h_tile2)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_na_tile3, h_tile3, sizeof(h_tile3)) != cudaSuccess)
     return VOSS_ERR_CUDA;
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
@@ -244,10 +255,10 @@ extern "C" int voss_primes_range_stats_noalloc(uint64_t a, uint64_t b, voss_rang
   prm.P = d.P;
   prm.M = d.M;
   prm.R = d.R;
-  prm.tileA = d.tileA;
-  prm.tileB = d.tileB;
-  prm.tile_a_stride16 = kNaTileAStride / 16;
-  prm.tile_b_stride16 = kNaTileBStride / 16;
+  for (int t = 0; t < kTiles; ++t) {
+    prm.tile[t] = d.tile[t];
+    prm.tile_stride16[t] = kNaTileStride[t] / 16;
+  }
   prm.seg_bytes = kNaSegBytes;
   prm.segs = sc->segs;
   prm.acc = &sc->acc;

@@ -3,12 +3,12 @@
 // One CTA owns one segment of S bytes (30*S integers) at a time, entirely in
 // shared memory, and takes (request, segment) items from a device work queue
 // (one global atomic per item; requests come heaviest first).  Per segment:
-//   1. fill: AND of two presieve tiles (primes 7..17 and 19..31) read at the
-//      segment's phase, 16 bytes per load from the tile copy in which that
-//      phase is aligned -- replaces the reference's memset + per-prime
+//   1. fill: AND of four presieve tiles (primes 7..17, 19..31, 37..43,
+//      47..59) read at the segment's phase, 16 bytes per load from the tile
+//      copy in which that phase is aligned -- replaces the reference's memset + per-prime
 //      launches for the smallest primes (context.cu:404-414);
 //   2. mark with shared-memory atomicAnd, in work units handed out heaviest
-//      first by a shared counter: primes 37 <= p < split one warp each
+//      first by a shared counter: primes 61 <= p < split one warp each
 //      (lane = residue class x stream, fixed bit mask per stream); split <=
 //      p < S four per warp-round (lane = prime x class); p >= S two per
 //      lane (at most one hit per class); primes from the request's bucket
@@ -176,8 +176,8 @@ __device__ __noinline__ void claim_item(unsigned long long* queue, const ReqDesc
     d.req = r; d.k0 = k0; d.nbytes = nb; d.np = a;
     d.split = R.tier_split; d.huge = R.tier_huge; d.rflags = R.rflags;
     uint32_t and0 = ~0u, or0 = 0u, keep0 = ~0u, keepl = ~0u;
-    if (k0 == 0) { and0 = 0xFFFFFE00u; or0 = 0x1FEu; }   // 1 no; 7..29, 31 yes
-    else if (k0 == 1) or0 = 1u;                            // 31
+    if (k0 == 0) { and0 = ~1u; or0 = kTilePrimeBits; }     // 1 no; the tile primes 7..59 yes
+    else if (k0 == 1) or0 = kTilePrimeBits >> 8;           // 31..59
     if (si == 0) {                                         // numbers below a
       for (uint32_t o = 0; o < 8; ++o)
         if (30ull * k0 + w30(o) < R.a) keep0 &= ~(1u << o);
@@ -260,16 +260,23 @@ sieve_segments_kernel(const SieveParams prm) {
     // 1. presieve fill
     {
       // copy (phase mod 16) of each tile holds the phase on a 16-byte boundary
-      const uint32_t phA = (uint32_t)(k0 % kTileAPeriod);
-      const uint32_t phB = (uint32_t)(k0 % kTileBPeriod);
-      const uint4* ta = reinterpret_cast<const uint4*>(prm.tileA) + (phA & 15u) * prm.tile_a_stride16 + (phA >> 4);
-      const uint4* tb = reinterpret_cast<const uint4*>(prm.tileB) + (phB & 15u) * prm.tile_b_stride16 + (phB >> 4);
+      uint32_t toff[kTiles];                       // 16-byte units from each tile's start
+#pragma unroll
+      for (int t = 0; t < kTiles; ++t) {
+        const uint32_t ph = (uint32_t)(k0 % tile_period(t));
+        toff[t] = (ph & 15u) * prm.tile_stride16[t] + (ph >> 4);
+      }
       uint4* seg4 = reinterpret_cast<uint4*>(seg);
       const uint32_t n16 = (nbytes + 15u) >> 4;    // up to 3 words past the end: never read
 #pragma unroll 4
       for (uint32_t v = tid; v < n16; v += nthr) {
-        const uint4 x = __ldg(ta + v), y = __ldg(tb + v);
-        seg4[v] = make_uint4(x.x & y.x, x.y & y.y, x.z & y.z, x.w & y.w);
+        uint4 x = __ldg(reinterpret_cast<const uint4*>(prm.tile[0]) + toff[0] + v);
+#pragma unroll
+        for (int t = 1; t < kTiles; ++t) {
+          const uint4 y = __ldg(reinterpret_cast<const uint4*>(prm.tile[t]) + toff[t] + v);
+          x.x &= y.x; x.y &= y.y; x.z &= y.z; x.w &= y.w;
+        }
+        seg4[v] = x;
       }
     }
     __syncthreads();

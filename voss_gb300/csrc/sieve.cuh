@@ -17,16 +17,42 @@ constexpr int kSmemBins = 256;        // bins kept in shared memory (gap < 512)
 constexpr int kSmemHistCopies = 8;    // one copy per 4 warps
 constexpr int kSmemStride = kSmemBins + 4;   // + the overflow bin, padded
 constexpr uint32_t kLargeGap = 500;   // the reference's large-gap threshold
-constexpr uint32_t kTileAPeriod = 7u * 11u * 13u * 17u;      // 17017 bytes
-constexpr uint32_t kTileBPeriod = 19u * 23u * 29u * 31u;     // 392863 bytes
-constexpr uint32_t kFirstTablePrime = 37;   // smallest prime not in a tile
+// Presieve tiles: the wheel bytes with the multiples of a few small primes
+// cleared are periodic, with period the product of those primes (in bytes).
+// Four tiles cover the primes 7..59.
+constexpr int kTiles = 4;
+constexpr uint32_t kTilePrimes[kTiles][4] = {{7, 11, 13, 17}, {19, 23, 29, 31}, {37, 41, 43, 0}, {47, 53, 59, 0}};
+__host__ __device__ constexpr uint32_t tile_period(int t) {
+  return t == 0 ? 7u * 11u * 13u * 17u      // 17017 bytes
+       : t == 1 ? 19u * 23u * 29u * 31u     // 392863 bytes
+       : t == 2 ? 37u * 41u * 43u           // 65231 bytes
+       :          47u * 53u * 59u;          // 146969 bytes
+}
+constexpr uint32_t kMaxTilePeriod = 19u * 23u * 29u * 31u;
+constexpr uint32_t kFirstTablePrime = 61;   // smallest prime not in a tile
+
+// The tile primes themselves (the tiles clear them as multiples of
+// themselves) as bits of the wheel's first two bytes, bit 8k + o for
+// 30k + W30[o]: 7..29 in byte 0, 31..59 in byte 1.
+constexpr uint32_t tile_prime_bits() {
+  uint32_t m = 0;
+  for (int t = 0; t < kTiles; ++t)
+    for (int i = 0; i < 4; ++i) {
+      const uint32_t q = kTilePrimes[t][i];
+      if (!q) continue;
+      for (uint32_t o = 0; o < 8; ++o)
+        if (((kW30Packed >> (8u * o)) & 0xFFu) == q % 30u) m |= 1u << (8u * (q / 30u) + o);
+    }
+  return m;
+}
+constexpr uint32_t kTilePrimeBits = tile_prime_bits();   // 0xDFFE
 constexpr int kMaxThreads = 1024;
 
-// The first kConstPrimes table primes (37, 41, 43, ...) with their Barrett
+// The first kConstPrimes table primes (61, 67, 71, ...) with their Barrett
 // constants floor((2^64-1)/p), computed at compile time.  Every prime table
 // the sieve kernel is given starts with exactly these; the kernel reads them
 // from constant memory, where a warp-uniform index is a broadcast.
-constexpr uint32_t kConstPrimes = 1024;      // primes 37 .. 8243
+constexpr uint32_t kConstPrimes = 1024;      // primes 61 .. 8293
 struct ConstPrimeTable {
   uint32_t p[kConstPrimes];
   unsigned long long m[kConstPrimes];
@@ -90,7 +116,7 @@ struct ReqDesc {
   uint64_t k_lo, k_hi;      // wheel bytes [k_lo, k_hi) that cover [a, b)
   uint64_t seg_base;        // index of the request's first segment
   uint64_t nseg;
-  uint32_t nprimes;         // table primes p (>= 37) with p*p < b
+  uint32_t nprimes;         // table primes p (>= 61) with p*p < b
   uint32_t seg_bytes;       // this request's segment size (<= the launch's)
   uint32_t tier_split;      // table index of the first mid-tier prime
   uint32_t tier_huge;       // table index of the first prime >= seg_bytes
@@ -184,13 +210,11 @@ struct SieveParams {
   const ReqDesc* reqs;
   const BatchHdr* hdr;
   unsigned long long* queue;   // work-queue head: next (request, segment) item
-  const uint32_t* P;         // table primes >= 37, ascending
+  const uint32_t* P;         // table primes >= 61, ascending
   const uint64_t* M;         // floor((2^64-1)/p), for x mod p
   const uint32_t* R;         // R[8 * i + o]: k = R (mod p) <=> p | 30k+W30[o] (32 B per prime)
-  const uint32_t* tileA;     // presieve tiles: kTileShifts shifted copies each
-  const uint32_t* tileB;
-  uint32_t tile_a_stride16;  // 16-byte units per copy of tile A
-  uint32_t tile_b_stride16;
+  const uint32_t* tile[kTiles];      // presieve tiles: kTileShifts shifted copies each
+  uint32_t tile_stride16[kTiles];    // 16-byte units per copy
   uint32_t seg_bytes;        // the largest segment of the launch (shared memory)
   SegRec* segs;
   ReqAccum* acc;
