@@ -80,7 +80,7 @@ int voss_gb300_cut_ranges(uint64_t n, const uint64_t* a, const uint64_t* b,
  * cudaMalloc / cudaFree would synchronize the device.  The reference has no
  * counterpart.  The call allocates nothing: its scratch, sieving-prime table
  * and presieve tiles live in static device arrays of this library (about
- * 19.4 MB per GPU that loads it, held until the process exits).  The caller
+ * 29.9 MB per GPU that loads it, held until the process exits).  The caller
  * passes the range and `out`, device-accessible memory that receives the
  * result in stream order on `stream` (a cudaStream_t, NULL = legacy default
  * stream); the call returns once the work is enqueued.
