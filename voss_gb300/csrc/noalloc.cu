@@ -42,12 +42,15 @@ constexpr uint32_t kNaPrimeLimit = 1u << 20;        // sieving primes, p*p < 2^4
 constexpr uint32_t kNaPrimes = 82008;               // primes in [61, 2^20)
 constexpr uint32_t kNaStride = 82016;               // kNaPrimes rounded up to 32
 constexpr uint32_t kNaLargeCap = 4096;
-// tile t: kTileShifts copies of kNaTileStride(t) bytes
-constexpr uint32_t kNaTileStride0 = tile_copy_stride(tile_period(0), kNaSegBytes);
-constexpr uint32_t kNaTileStride1 = tile_copy_stride(tile_period(1), kNaSegBytes);
-constexpr uint32_t kNaTileStride2 = tile_copy_stride(tile_period(2), kNaSegBytes);
-constexpr uint32_t kNaTileStride3 = tile_copy_stride(tile_period(3), kNaSegBytes);
-constexpr uint32_t kNaTileStride[kTiles] = {kNaTileStride0, kNaTileStride1, kNaTileStride2, kNaTileStride3};
+// All tiles in one block: tile t is kTileShifts copies of
+// tile_copy_stride(tile_period(t), kNaSegBytes) bytes, from byte
+// na_tile_offset(t).
+constexpr uint64_t na_tile_offset(int t) {
+  uint64_t off = 0;
+  for (int i = 0; i < t; ++i) off += (uint64_t)kTileShifts * tile_copy_stride(tile_period(i), kNaSegBytes);
+  return off;
+}
+constexpr uint64_t kNaTileBytes = na_tile_offset(kTiles);
 
 struct NaScratch {
   BatchHdr hdr;
@@ -68,20 +71,13 @@ static __device__ __align__(256) unsigned char g_na_scratch[sizeof(NaScratch)];
 static __device__ __align__(256) uint32_t g_na_P[kNaStride];
 static __device__ __align__(256) uint64_t g_na_M[kNaStride];
 static __device__ __align__(256) uint32_t g_na_R[8 * kNaStride];
-static __device__ __align__(256) uint32_t g_na_tile0[kTileShifts * kNaTileStride0 / 4];
-static __device__ __align__(256) uint32_t g_na_tile1[kTileShifts * kNaTileStride1 / 4];
-static __device__ __align__(256) uint32_t g_na_tile2[kTileShifts * kNaTileStride2 / 4];
-static __device__ __align__(256) uint32_t g_na_tile3[kTileShifts * kNaTileStride3 / 4];
+static __device__ __align__(256) uint32_t g_na_tiles[kNaTileBytes / 4];
 
 // Host copies of the tables, built once per process in static storage.
 static uint32_t h_P[kNaStride];
 static uint64_t h_M[kNaStride];
 static uint32_t h_R[8 * kNaStride];
-static uint8_t h_tile0[kTileShifts * kNaTileStride0];
-static uint8_t h_tile1[kTileShifts * kNaTileStride1];
-static uint8_t h_tile2[kTileShifts * kNaTileStride2];
-static uint8_t h_tile3[kTileShifts * kNaTileStride3];
-static uint8_t* const h_tile[kTiles] = {h_tile0, h_tile1, h_tile2, h_tile3};
+static uint8_t h_tiles[kNaTileBytes];
 static uint8_t h_tile_base[kMaxTilePeriod];    // one period of a tile
 static uint8_t h_comp[kNaPrimeLimit];
 static bool h_built = false;
@@ -89,8 +85,7 @@ static bool h_built = false;
 struct NaDevice {
   bool ready = false;
   NaScratch* scratch = nullptr;
-  uint32_t *P = nullptr, *R = nullptr;
-  uint32_t* tile[kTiles] = {};
+  uint32_t *P = nullptr, *R = nullptr, *tiles = nullptr;
   uint64_t* M = nullptr;
   uint32_t sms = 0;
 };
@@ -126,8 +121,8 @@ void build_host_tables() {
     ++n;
   }
   for (int t = 0; t < kTiles; ++t)
-    build_tile_copies(kTilePrimes[t], kTilePrimes[t][3] ? 4 : 3, tile_period(t), kNaTileStride[t], h_tile_base,
-                      h_tile[t]);
+    build_tile_copies(kTilePrimes[t], kTilePrimes[t][3] ? 4 : 3, tile_period(t),
+                      tile_copy_stride(tile_period(t), kNaSegBytes), h_tile_base, h_tiles + na_tile_offset(t));
   h_built = (n == kNaPrimes);
 }
 
@@ -145,16 +140,12 @@ int setup(int dev) {
   if (!h_built) return VOSS_ERR_INTERNAL;
   if (symbol_ptr(&d.scratch, g_na_scratch) != cudaSuccess || symbol_ptr(&d.P, g_na_P) != cudaSuccess ||
       symbol_ptr(&d.M, g_na_M) != cudaSuccess || symbol_ptr(&d.R, g_na_R) != cudaSuccess ||
-      symbol_ptr(&d.tile[0], g_na_tile0) != cudaSuccess || symbol_ptr(&d.tile[1], g_na_tile1) != cudaSuccess ||
-      symbol_ptr(&d.tile[2], g_na_tile2) != cudaSuccess || symbol_ptr(&d.tile[3], g_na_tile3) != cudaSuccess)
+      symbol_ptr(&d.tiles, g_na_tiles) != cudaSuccess)
     return VOSS_ERR_CUDA;
   if (cudaMemcpyToSymbol(g_na_P, h_P, sizeof(h_P)) != cudaSuccess ||
       cudaMemcpyToSymbol(g_na_M, h_M, sizeof(h_M)) != cudaSuccess ||
       cudaMemcpyToSymbol(g_na_R, h_R, sizeof(h_R)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_na_tile0, h_tile0, sizeof(h_tile0)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_na_tile1, h_tile1, sizeof(h_tile1)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_na_tile2, h_tile2, sizeof(h_tile2)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_na_tile3, h_tile3, sizeof(h_tile3)) != cudaSuccess)
+      cudaMemcpyToSymbol(g_na_tiles, h_tiles, sizeof(h_tiles)) != cudaSuccess)
     return VOSS_ERR_CUDA;
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
@@ -256,8 +247,8 @@ extern "C" int voss_primes_range_stats_noalloc(uint64_t a, uint64_t b, voss_rang
   prm.M = d.M;
   prm.R = d.R;
   for (int t = 0; t < kTiles; ++t) {
-    prm.tile[t] = d.tile[t];
-    prm.tile_stride16[t] = kNaTileStride[t] / 16;
+    prm.tile[t] = d.tiles + na_tile_offset(t) / 4;
+    prm.tile_stride16[t] = tile_copy_stride(tile_period(t), kNaSegBytes) / 16;
   }
   prm.seg_bytes = kNaSegBytes;
   prm.segs = sc->segs;

@@ -176,8 +176,8 @@ __device__ __noinline__ void claim_item(unsigned long long* queue, const ReqDesc
     d.req = r; d.k0 = k0; d.nbytes = nb; d.np = a;
     d.split = R.tier_split; d.huge = R.tier_huge; d.rflags = R.rflags;
     uint32_t and0 = ~0u, or0 = 0u, keep0 = ~0u, keepl = ~0u;
-    if (k0 == 0) { and0 = ~1u; or0 = kTilePrimeBits; }     // 1 no; the tile primes 7..59 yes
-    else if (k0 == 1) or0 = kTilePrimeBits >> 8;           // 31..59
+    if (k0 == 0) and0 = ~1u;                               // 1 is not prime
+    if (k0 < 3) or0 = (uint32_t)(kTilePrimeBits >> (8u * k0));   // the tile primes are
     if (si == 0) {                                         // numbers below a
       for (uint32_t o = 0; o < 8; ++o)
         if (30ull * k0 + w30(o) < R.a) keep0 &= ~(1u << o);

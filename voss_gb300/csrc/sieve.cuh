@@ -32,20 +32,22 @@ constexpr uint32_t kMaxTilePeriod = 19u * 23u * 29u * 31u;
 constexpr uint32_t kFirstTablePrime = 61;   // smallest prime not in a tile
 
 // The tile primes themselves (the tiles clear them as multiples of
-// themselves) as bits of the wheel's first two bytes, bit 8k + o for
-// 30k + W30[o]: 7..29 in byte 0, 31..59 in byte 1.
-constexpr uint32_t tile_prime_bits() {
-  uint32_t m = 0;
+// themselves) as bits of the wheel's first bytes, bit 8k + o for
+// 30k + W30[o]: 7..29 in byte 0, 31..59 in byte 1.  All tile primes are
+// below 90 (bytes 0..2), which the segment fix-ups rely on.
+constexpr uint64_t tile_prime_bits() {
+  uint64_t m = 0;
   for (int t = 0; t < kTiles; ++t)
     for (int i = 0; i < 4; ++i) {
       const uint32_t q = kTilePrimes[t][i];
       if (!q) continue;
       for (uint32_t o = 0; o < 8; ++o)
-        if (((kW30Packed >> (8u * o)) & 0xFFu) == q % 30u) m |= 1u << (8u * (q / 30u) + o);
+        if (((kW30Packed >> (8u * o)) & 0xFFu) == q % 30u) m |= 1ull << (8u * (q / 30u) + o);
     }
   return m;
 }
-constexpr uint32_t kTilePrimeBits = tile_prime_bits();   // 0xDFFE
+constexpr uint64_t kTilePrimeBits = tile_prime_bits();
+static_assert(kTilePrimeBits < (1ull << 24), "tile primes must lie in the wheel's first three bytes");
 constexpr int kMaxThreads = 1024;
 
 // The first kConstPrimes table primes (61, 67, 71, ...) with their Barrett
