@@ -36,7 +36,7 @@ REGIMES = [
     (MAX_B, U64_MAX, [(10**14, 10**14 + 10**9), (10**14 - 10**10, 10**14)]),
 ]
 SEGS = [65536, 98304, 131072, 163840, 196608, 221184]
-SPLITS = [1024, 2048, 3072, 4096, 6144, 12288]
+SPLITS = [512, 768, 1024, 2048, 3072, 4096, 6144, 12288]
 BUCKETS = [0, 221184, 442368, 884736, 1769472]   # bucket-list split (0 = none)
 BUCKET_MARGIN = 0.97                              # a split must beat no lists by 3%
 
@@ -75,7 +75,7 @@ def run(quick=False, write=False, out=sys.stdout):
     lib.voss_gb300_set_tuning.argtypes = [ctypes.c_uint32, ctypes.POINTER(TuneEntry)]
     stream = torch.cuda.Stream()
     segs = SEGS[-3:] if quick else SEGS
-    splits = SPLITS[1:4] if quick else SPLITS
+    splits = SPLITS[2:5] if quick else SPLITS
     buckets = BUCKETS[:3] if quick else BUCKETS
     table = []
     for b_max, w_max, ranges in REGIMES:
