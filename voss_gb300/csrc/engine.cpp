@@ -69,7 +69,7 @@ HostPinned::~HostPinned() {
 
 static const uint32_t kW30[8] = {1, 7, 11, 13, 17, 19, 23, 29};
 // Largest segment any config may use; tiles are extended by this much.
-static const uint32_t kMaxSegBytes = 221184;
+static const uint32_t kMaxSegBytes = 226944;
 
 static int64_t inverse_mod(int64_t a, int64_t m) {
   int64_t t = 0, nt = 1, r = m, nr = a % m;

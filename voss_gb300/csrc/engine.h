@@ -51,7 +51,7 @@ struct HostPinned {
 };
 
 struct Config {
-  uint32_t seg_bytes = 221184;    // 216 KiB: the largest that fits with the histograms
+  uint32_t seg_bytes = 226944;    // the largest that fits with the histograms (227 KB per CTA)
   uint32_t threads = 1024;
   uint32_t tier_split = 6144;    // primes below: a warp per prime; above: 4 per warp
   uint32_t ctas_per_sm = 1;

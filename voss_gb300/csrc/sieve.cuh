@@ -14,7 +14,7 @@ namespace vg {
 constexpr uint64_t kW30Packed = 0x1D1713110D0B0701ull;  // W30[o] = byte o
 constexpr int kHistBins = 1025;       // gap/2 bins 0..1023, bin 1024 = gap >= 2048
 constexpr int kSmemBins = 256;        // bins kept in shared memory (gap < 512)
-constexpr int kSmemHistCopies = 8;    // one copy per 4 warps
+constexpr int kSmemHistCopies = 4;    // one copy per 8 warps
 constexpr int kSmemStride = kSmemBins + 4;   // + the overflow bin, padded
 constexpr uint32_t kLargeGap = 500;   // the reference's large-gap threshold
 // Presieve tiles: the wheel bytes with the multiples of a few small primes
