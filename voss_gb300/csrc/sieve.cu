@@ -285,12 +285,14 @@ sieve_segments_kernel(const SieveParams prm) {
     //    units [0, nsmall): one prime each, p < split: a warp per prime, lane
     //      = (class o, stream h of 4); a stream steps 4p bytes = p words, so
     //      its bit mask never changes;
-    //    units [nsmall, ...): 32 primes each, p >= split: lanes = (prime q of
-    //      4, class o), eight rounds of four primes, loads of all rounds
-    //      issued before any marking so their latency overlaps.
+    //    then 32 primes each, split <= p < S: lanes = (prime q of 4, class
+    //      o), eight rounds of four primes, loads of all rounds issued before
+    //      any marking so their latency overlaps;
+    //    then 64 primes each, p >= S (two per lane), then the bucket units.
     {
       // unit layout: [0, nsmall) small primes, then 32-prime units of the mid
-      // tier (split <= p < S), then 32-prime units of the huge tier (p >= S)
+      // tier (split <= p < S), then 64-prime units of the huge tier (p >= S),
+      // then kBucketUnit-entry units of the segment's bucket list
       const uint32_t nsmall = S.split < np ? S.split : np;
       const uint32_t hbeg = S.huge < np ? max(S.huge, nsmall) : np;
       const uint32_t nmidu = (hbeg - nsmall + 31u) / 32u;
