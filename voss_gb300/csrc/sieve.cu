@@ -322,7 +322,7 @@ sieve_segments_kernel(const SieveParams prm) {
             const uint32_t mask = ~(1u << ((c << 3) | o));
             const uint32_t lim = (nbytes - c + 3u) >> 2;
             uint32_t w = j0 >> 2;
-#pragma unroll 16
+#pragma unroll 32
             for (; w < lim; w += p) atomicAnd(seg + w, mask);
           }
         } else if (u >= nscan) {
@@ -398,7 +398,7 @@ sieve_segments_kernel(const SieveParams prm) {
             if (!p) continue;
             uint32_t s = rr[t] >= m ? rr[t] - m : rr[t] + p - m;
             if (low_any && 30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
-#pragma unroll 4
+#pragma unroll 8
             for (uint32_t j = s; j < nbytes; j += p) clear_bit(seg, j, keep);
           }
         }
