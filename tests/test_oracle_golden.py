@@ -5,9 +5,6 @@
 2. Against the known answers in the reference's tests
    (library/tests/test_primes.py, test_prime_count.cpp, sanitizer_test.cpp).
 """
-import math
-
-import numpy as np
 import pytest
 
 

@@ -4,7 +4,6 @@ small accumulators and stitch them.  The result must equal the whole range."""
 import os
 import socket
 
-import numpy as np
 import pytest
 
 
