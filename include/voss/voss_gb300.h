@@ -98,7 +98,9 @@ int voss_primes_range_stats_noalloc(uint64_t a, uint64_t b, voss_range_stats_t* 
  * size (multiple of 32, <= 1024).  tier_split: primes below it are marked a
  * warp per prime, primes from it on four primes per warp.  ctas_per_sm: resident
  * CTAs per SM used to size the persistent grid.  Zero fields keep the
- * current value; auto_tune = 1 lets the library pick per range. */
+ * current value; auto_tune = 1 lets the library pick per range.
+ * set_config and set_tuning return VOSS_ERR_INVALID_ARG while a request
+ * server runs on the device (its thread reads both). */
 typedef struct {
     uint32_t seg_bytes;
     uint32_t threads;

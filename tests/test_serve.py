@@ -85,3 +85,17 @@ def test_shared_and_isolated_servers_agree(vg):
         alone, _, _ = run_served(srv, reqs)
     for r, x, y in zip(reqs, shared, alone):
         assert same_answer(r, x, y), (r, x, y)
+
+
+@pytest.mark.gpu
+def test_config_is_frozen_while_a_server_runs(vg):
+    """The server's thread reads the engine's configuration and tuning table,
+    so neither may change while a server is alive."""
+    from voss_gb300.serve import Server
+    base = vg.primes.get_config()
+    with Server(slots=1) as srv:
+        with pytest.raises(vg.VossError):
+            vg.primes.set_config(**base)
+        got, _ = srv.result(srv.submit(0, 1000, 0))
+        assert got.count == 168
+    vg.primes.set_config(**base)                # allowed again once it is gone

@@ -704,6 +704,7 @@ extern "C" int voss_gb300_set_config(const voss_gb300_config_t* c) {
   return guarded([&] {
     vg::Engine& E = vg::Engine::for_current_device();
     std::lock_guard<std::mutex> g(E.mu);
+    if (E.servers) throw vg::Error(VOSS_ERR_INVALID_ARG, "a request server is running on this device");
     vg::Config n = E.cfg;
     if (c->seg_bytes) n.seg_bytes = c->seg_bytes;
     if (c->threads) n.threads = c->threads;
@@ -730,6 +731,7 @@ extern "C" int voss_gb300_set_tuning(uint32_t n, const voss_gb300_tune_entry_t* 
   return guarded([&] {
     vg::Engine& E = vg::Engine::for_current_device();
     std::lock_guard<std::mutex> g(E.mu);
+    if (E.servers) throw vg::Error(VOSS_ERR_INVALID_ARG, "a request server is running on this device");
     E.tuning.clear();
     for (uint32_t i = 0; i < n; ++i)
       E.tuning.push_back(vg::TuneEntry{e[i].b_max, e[i].width_max, e[i].seg_bytes, e[i].tier_split,

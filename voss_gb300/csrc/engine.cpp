@@ -282,7 +282,11 @@ void Plan::reserve_capacity(uint32_t max_req, uint64_t max_segs, uint64_t max_bu
 }
 
 uint64_t Plan::bucket_bytes_for(uint64_t a, uint64_t b) const {
-  if (b <= a || !allow_buckets) return 0;
+  return allow_buckets ? list_bytes_for(a, b) : 0;
+}
+
+uint64_t Plan::list_bytes_for(uint64_t a, uint64_t b) const {
+  if (b <= a) return 0;
   Engine& E = *eng;
   const Config c = E.tuned_for(a, b, batch_mode);
   const uint64_t bytes = (b + 29) / 30 - a / 30;

@@ -162,8 +162,12 @@ struct Plan {
   void kernel_ms(float* sieve_ms, float* finalize_ms);
   // Segments a range needs under this plan's tuning (for admission).
   uint64_t segments_for(uint64_t a, uint64_t b) const;
-  // Bucket-list bytes a range needs under this plan's tuning (for admission).
+  // Bucket-list bytes a range needs under this plan's tuning (for admission);
+  // 0 while the plan runs without lists.
   uint64_t bucket_bytes_for(uint64_t a, uint64_t b) const;
+  // The same when lists are allowed; reads no mutable plan state, so another
+  // thread may call it while this plan runs.
+  uint64_t list_bytes_for(uint64_t a, uint64_t b) const;
   // True if the last run's bucket lists overflowed (its results are then
   // invalid); valid once the stream has passed fetch_async().
   bool overflowed() const;
@@ -200,6 +204,9 @@ class Engine {
   std::string name;
   cudaStream_t stream = nullptr;
   Config cfg;
+  // Request servers alive on this engine (guarded by mu).  Their threads read
+  // cfg and tuning without mu, so neither may change while one runs.
+  int servers = 0;
 
   // Resident sieving-prime table: primes >= 61 up to table_limit.
   std::vector<uint32_t> hP;

@@ -61,6 +61,8 @@ Server::Server(Engine& e, const ServerConfig& c) : E(e), cfg(c) {
     check_cuda(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "server event");
   }
   worker = std::thread([this] { loop(); });
+  std::lock_guard<std::mutex> g(E.mu);
+  ++E.servers;
 }
 
 Server::~Server() {
@@ -70,6 +72,10 @@ Server::~Server() {
   }
   cv_work.notify_all();
   if (worker.joinable()) worker.join();
+  {
+    std::lock_guard<std::mutex> g(E.mu);
+    --E.servers;
+  }
   for (auto& sp : slots) {
     if (sp->stream) {
       cudaStreamSynchronize(sp->stream);
@@ -91,7 +97,7 @@ uint64_t Server::submit(uint64_t a, uint64_t b, uint32_t op) {
   t.op = op;
   t.segs = segs;
   // bucket lists that do not fit a slot's arena are not used (the plan skips them)
-  uint64_t bb = slots[0]->plan.bucket_bytes_for(a, b);
+  uint64_t bb = slots[0]->plan.list_bytes_for(a, b);
   if (bb > cfg.bucket_bytes) bb = 0;
   t.bytes = request_bytes(segs) + bb;
   t.t_submit = now_us();
