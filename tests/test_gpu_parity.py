@@ -10,6 +10,8 @@ import random
 import numpy as np
 import pytest
 
+from conftest import ROOT
+
 pytestmark = pytest.mark.gpu
 
 EXACT_KEYS = ("count", "pi_4_1", "pi_4_3", "pi_3_1", "pi_3_2", "max_gap", "max_gap_start", "num_gaps")
@@ -408,3 +410,26 @@ def test_batch_in_chunks(vg):
         alone = vg.range_stats(a, b)
         for k in PUBLIC_KEYS:
             assert getattr(got[i], k) == getattr(alone, k), (i, a, b, k)
+
+
+@pytest.mark.gpu
+def test_plan_survives_table_growth(vg):
+    """A plan keeps the prime table it was built with: growing the table for
+    a larger range afterwards leaves the plan's results unchanged.  Runs in a
+    fresh process, where the table starts small."""
+    import subprocess
+    import sys
+    code = (
+        "import sys; sys.path.insert(0, %r)\n"
+        "import torch\n"
+        "import voss_gb300 as vg\n"
+        "from voss_gb300.plan import SievePlan\n"
+        "st = torch.cuda.Stream()\n"
+        "p = SievePlan([(10**9, 10**9 + 10**8)])\n"
+        "p.launch(st.cuda_stream); r1 = p.results(st.cuda_stream)[0]\n"
+        "vg.range_stats(10**14, 10**14 + 10**6)\n"
+        "p.launch(st.cuda_stream); r2 = p.results(st.cuda_stream)[0]\n"
+        "assert (r1.count, r1.max_gap, r1.twins) == (r2.count, r2.max_gap, r2.twins), (r1, r2)\n"
+        "print(r1.count)\n" % str(ROOT))
+    out = subprocess.run([sys.executable, "-c", code], check=True, capture_output=True, text=True, timeout=600)
+    assert int(out.stdout.split()[-1]) > 0

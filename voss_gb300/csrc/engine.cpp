@@ -165,8 +165,17 @@ void Engine::ensure_table(uint64_t pmax) {
   for (size_t i = 0; i < std::min<size_t>(n, kConstPrimes); ++i)
     if (P[i] != kConstTable.p[i] || M[i] != kConstTable.m[i])
       throw Error(VOSS_ERR_INTERNAL, "prime table differs from the kernel's constant table");
-  // Plans launched earlier may still read the old table.
-  check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize(table)");
+  // Plans built earlier keep pointers to the current table: it is retired,
+  // not freed, and stays valid for them.
+  for (DevBuf* d : {&dP, &dM, &dR}) {
+    if (!d->ptr) continue;
+    std::unique_ptr<DevBuf> old(new DevBuf());
+    old->ptr = d->ptr;
+    old->bytes = d->bytes;
+    d->ptr = nullptr;
+    d->bytes = 0;
+    retired_tables.push_back(std::move(old));
+  }
   dP.reserve(std::max<size_t>(n, 1) * 4);
   dM.reserve(std::max<size_t>(n, 1) * 8);
   dR.reserve(std::max<size_t>(n, 1) * 8 * 4);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -213,6 +214,10 @@ class Engine {
   std::vector<double> hInvPrefix;   // sum of 1/p over table primes [0, i)
   uint64_t table_limit = 0;
   DevBuf dP, dM, dR;            // primes, Barrett constants, class residues (8 per prime)
+  // Earlier, smaller copies of the table.  Plans keep pointers to the table
+  // they were built with, so a grown table leaves the old one allocated (its
+  // primes are a prefix of the new one's) until the engine goes.
+  std::vector<std::unique_ptr<DevBuf>> retired_tables;
   DevBuf tile[kTiles];        // presieve tiles, kTileShifts shifted copies each
 
   // Scratch plan reused by the synchronous entry points.
