@@ -46,7 +46,7 @@ CHUNK = 25 * 10**7       # integers per chunk when the range is dealt over ranks
 # The reference's published A100 times for the same calls (its README and
 # STATE notes): Context(10^10) STANDARD, and the Goldbach check to 10^9.
 PUBLISHED_MS = {"C2 [0,1e10)": 530.0, "C4": 2200.0}
-# Context(10^12) STANDARD (count + gaps), 62.3 s on an A100
+# The reference's published Context(10^12) STANDARD (count + gaps) time: 62.3 s on an A100 (STATE.md:76-77)
 PUBLISHED_INT_PER_S = 10**12 / 62.3
 
 
@@ -194,7 +194,7 @@ def time_plan(plan, stream, torch, steps, flush, kernel_times=None):
 
 
 def secondary(torch, stream, flush):
-    """Other BASELINE configs, timed on the device (not the headline)."""
+    """The other workloads (C1-C5), timed on the device (not the headline)."""
     from voss_gb300.plan import GoldbachPlan, SievePlan
     out = {}
     cases = {"C1 [0,1e7)": (0, 10**7), "C2 [0,1e10)": (0, 10**10),

@@ -63,7 +63,7 @@ def test_golden_context(vg, golden):
                                   (10**7, 664579), (10**8, 5761455), (10**9, 50847534),
                                   (10**10, 455052511)])
 def test_prime_count_known(vg, N, pi):
-    # test_primes.py:45-55, BASELINE pi(10^10)
+    # test_primes.py:45-55; pi(10^10) = 455 052 511 (the reference's headline count)
     assert vg.primes.prime_count(N) == pi
 
 
@@ -178,7 +178,7 @@ def test_large_gaps_and_boundaries(vg, oracle_lib):
 
 
 def test_context_1e12_reference_values(vg):
-    """pi(10^12) (BASELINE) and the reference's large-gap list to 10^12: 11
+    """pi(10^12) = 37 607 912 018 and the reference's large-gap list to 10^12: 11
     gaps >= 500, the largest 540 ending at 738 832 928 467
     (test_primes.py:438-458)."""
     with vg.Context(10**12) as ctx:

@@ -86,7 +86,7 @@ def test_reference_in_range_values(oracle_lib):
 
 
 def test_pi_1e10(oracle_lib):
-    # BASELINE: pi(10^10) = 455052511
+    # pi(10^10) = 455052511, the reference's headline count
     assert oracle_lib.range_stats(0, 10**10)["count"] == 455052511
 
 
