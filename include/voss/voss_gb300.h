@@ -89,7 +89,11 @@ int voss_gb300_cut_ranges(uint64_t n, const uint64_t* a, const uint64_t* b,
  * The first call on a device sets that device up; make it before any stream
  * capture.  All calls share one scratch array and leave their contents
  * behind: calls in sequence are independent, calls that overlap on the GPU
- * race and give wrong results. */
+ * race and give wrong results.
+ * Errors: a refused launch shows in the return code; a fault while the
+ * kernels run surfaces on the caller's next synchronisation of `stream`.
+ * If a CUDA error is already pending on the calling thread, the call
+ * returns VOSS_ERR_CUDA without launching and leaves that error in place. */
 int voss_primes_range_stats_noalloc(uint64_t a, uint64_t b, voss_range_stats_t* out,
                                     void* stream);
 

@@ -1,6 +1,7 @@
 """Generate the golden fixtures in this folder from the reference's own oracle.
 
-Run in a checkout where the voss reference tree is available:
+Run where a checkout of the voss reference is available, naming its top
+folder (the one holding library/) as the argument or in VOSS_REFERENCE_ROOT:
 
     python tests/golden/make_golden.py /path/to/voss
 
@@ -14,6 +15,7 @@ the maximal gap, and the smallest Goldbach prime.  The output is
 from __future__ import annotations
 
 import json
+import os
 import random
 import sys
 from pathlib import Path
@@ -42,7 +44,11 @@ def window_stats(sympy, a: int, b: int) -> dict:
 
 
 def main() -> None:
-    ref_root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VOSS_REFERENCE_ROOT")
+    if not arg:
+        raise SystemExit("name the reference checkout: make_golden.py /path/to/voss "
+                         "(or set VOSS_REFERENCE_ROOT)")
+    ref_root = Path(arg)
     sys.path.insert(0, str(ref_root / "library" / "tests"))
     import reference as ref  # the reference's sympy oracle
     import sympy

@@ -143,10 +143,14 @@ def test_python_mirror_validation():
         v.conjectures.test_goldbach_upto(None)
 
 
-REF_BINDINGS = Path("/root/reference/library/bindings/python")
+# The reference checkout, when one is available: VOSS_REFERENCE_ROOT names its
+# top folder (the one holding library/).
+_REF_ROOT = os.environ.get("VOSS_REFERENCE_ROOT")
+REF_BINDINGS = Path(_REF_ROOT) / "library" / "bindings" / "python" if _REF_ROOT else None
 
 
-@pytest.mark.skipif(not REF_BINDINGS.exists(), reason="reference tree not mounted here")
+@pytest.mark.skipif(REF_BINDINGS is None or not REF_BINDINGS.exists(),
+                    reason="VOSS_REFERENCE_ROOT is unset or holds no library/bindings/python")
 def test_reference_binding_loads_this_library(lib):
     """The unmodified reference ctypes package binds this libvoss.so and its
     validation-only behaviour matches (the reference's non-GPU tests)."""

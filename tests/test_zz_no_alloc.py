@@ -51,3 +51,25 @@ def test_noalloc_rejects_beyond_its_limits(vg):
     assert lib.voss_primes_range_stats_noalloc(0, (1 << 40) + 1, ptr, stream) == 2     # b > 2^40
     assert lib.voss_primes_range_stats_noalloc(0, 5 * 10**11, ptr, stream) == 2        # > 65536 segments
     assert lib.voss_primes_range_stats_noalloc(0, 100, None, stream) == 6               # no output
+
+
+def test_noalloc_leaves_device_memory_alone_once_set_up(vg):
+    """The promise itself: after the first call on a device (its set-up),
+    further calls leave the device's free memory exactly where it was.
+    Nothing else allocates between the two readings."""
+    import torch
+    from voss_gb300 import _capi
+    lib = _capi._lib
+    out = torch.zeros(ctypes.sizeof(_capi.VossRangeStats), dtype=torch.uint8, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ptr = ctypes.c_void_p(out.data_ptr())
+    assert lib.voss_primes_range_stats_noalloc(0, 10**9, ptr, stream) == 0      # set-up, kernels loaded
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    counts = []
+    for a, b in ((10**11, 10**11 + 10**10), (7, 10**6), (0, 10**10), (0, 10**10)):
+        assert lib.voss_primes_range_stats_noalloc(a, b, ptr, stream) == 0, (a, b)
+        torch.cuda.synchronize()
+        counts.append(_capi.VossRangeStats.from_buffer_copy(out.cpu().numpy().tobytes()).count)
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert counts[2] == counts[3] == 455052511 and counts[1] == 78498 - 3

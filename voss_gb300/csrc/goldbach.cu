@@ -21,6 +21,7 @@
 #include <memory>
 #include <vector>
 
+#include "attr_cache.h"
 #include "goldbach.h"
 #include "voss/voss.h"
 
@@ -370,12 +371,13 @@ void goldbach_plan_launch(GoldbachPlan* g, cudaStream_t s) {
   o.err = reinterpret_cast<unsigned int*>(sc + 4);
   o.ce = g->ce.as<unsigned long long>();
   o.ce_cap = g->ce_cap;
-  static bool attr_set = false;
-  if (!attr_set) {
-    check_cuda(cudaFuncSetAttribute(goldbach_minp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kGbSmemBytes), "goldbach smem");
-    attr_set = true;
-  }
+  static AttrCache attr;          // per device, thread-safe
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  check_cuda((cudaError_t)attr.ensure(dev, kGbSmemBytes, [](size_t n) {
+               return (int)cudaFuncSetAttribute(goldbach_minp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)n);
+             }), "goldbach smem");
   goldbach_minp_kernel<<<g->grid, kGbThreads, kGbSmemBytes, s>>>(odd, g->oddp.as<uint32_t>(), kGoldbachPrimes,
                                                                   g->N, g->ntiles, o);
   check_cuda(cudaGetLastError(), "goldbach_minp_kernel");

@@ -8,8 +8,10 @@
 // serves them: it runs the same sieve and finalize kernels as
 // voss_primes_range_stats, but every byte of device memory it uses beyond
 // the caller's output lives in file-scope static __device__ arrays below
-// (about 6.6 MB per GPU that loads this library, held until the process
-// exits).  It calls no cudaMalloc, cudaFree or allocating library routine.
+// (about 29.9 MB per GPU that loads this library, held until the process
+// exits: 24.1 MB of presieve tile copies, 3.6 MB of sieving-prime table and
+// 2.2 MB of scratch).  It calls no cudaMalloc, cudaFree or allocating library
+// routine.
 //
 // Limits (checked, VOSS_ERR_OUT_OF_RANGE beyond them): b <= 2^40, and at
 // most kNaMaxSegs segments of 221184 bytes (30 integers each), i.e. a range
@@ -22,6 +24,12 @@
 // in sequence are independent, but calls that overlap on the GPU (different
 // streams, or different host threads at once) race on the scratch and give
 // wrong results.
+//
+// Errors: the call returns once its kernels are enqueued.  A launch that is
+// refused shows in its return code; a fault while the kernels run surfaces
+// on the caller's next synchronisation of the stream.  An error already
+// pending on the calling thread when the call starts is left in place for
+// the caller to read, and the call returns VOSS_ERR_CUDA without launching.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -64,9 +72,10 @@ struct NaScratch {
   SegRec segs[kNaMaxSegs];
 };
 
-// The scratch of every call (about 2.2 MB) and the resident tables (about
-// 4.4 MB).  In host code these names are host-side stand-ins; their device
-// addresses come from cudaGetSymbolAddress at set-up.
+// The scratch of every call (about 2.2 MB), the sieving-prime table (P, M
+// and R: about 3.6 MB) and the presieve tile copies (about 24.1 MB).  In
+// host code these names are host-side stand-ins; their device addresses
+// come from cudaGetSymbolAddress at set-up.
 static __device__ __align__(256) unsigned char g_na_scratch[sizeof(NaScratch)];
 static __device__ __align__(256) uint32_t g_na_P[kNaStride];
 static __device__ __align__(256) uint64_t g_na_M[kNaStride];
@@ -206,6 +215,9 @@ extern "C" int voss_primes_range_stats_noalloc(uint64_t a, uint64_t b, voss_rang
   using namespace vg;
   if (!out) return VOSS_ERR_INVALID_ARG;
   if (b > kNaMaxB) return VOSS_ERR_OUT_OF_RANGE;
+  // an error left by earlier work on this thread stays for its owner to
+  // read (the launch checks below would otherwise take it as this call's)
+  if (cudaPeekAtLastError() != cudaSuccess) return VOSS_ERR_CUDA;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return VOSS_ERR_NO_CUDA;
   const int rc = setup(dev);

@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "attr_cache.h"
 #include "sieve.cuh"
 
 namespace vg {
@@ -848,13 +849,16 @@ size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads) {
 cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads,
                          cudaStream_t stream) {
   const size_t smem = sieve_smem_bytes(prm.seg_bytes, threads);
-  static size_t smem_set = 0;   // raised once per size, outside stream capture
-  if (smem > smem_set) {
-    cudaError_t e = cudaFuncSetAttribute(sieve_segments_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    smem_set = smem;
-  }
+  // the attribute is per device: raised once per (device, size), outside
+  // stream capture (plans raise it before they capture)
+  static AttrCache attr;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const int rc = attr.ensure(dev, smem, [](size_t n) {
+    return (int)cudaFuncSetAttribute(sieve_segments_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)n);
+  });
+  if (rc) return (cudaError_t)rc;
   if (grid == 0) return cudaSuccess;
   sieve_segments_kernel<<<grid, threads, smem, stream>>>(prm);
   return cudaGetLastError();
