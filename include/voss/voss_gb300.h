@@ -153,8 +153,9 @@ int voss_gb300_plan_launch(voss_gb300_plan* plan, void* stream);
 /* Copy the results of the last run to the host (synchronises `stream`). */
 int voss_gb300_plan_results(voss_gb300_plan* plan, voss_range_stats_t* out, void* stream);
 /* Segments, grid size, kernels per run, shared bytes per CTA, and the
- * algorithmic work of one run: candidate clears by primes >= 37, and the
- * wheel bytes covered. */
+ * algorithmic work of one run: the candidate clears of Eratosthenes by the
+ * primes 17 < p <= sqrt(b) of each range (whether the presieve tiles or the
+ * marking does them), and the wheel bytes covered. */
 int voss_gb300_plan_info(voss_gb300_plan* plan, uint64_t* total_segments, uint32_t* grid,
                          uint32_t* kernels_per_run, uint32_t* smem_bytes,
                          uint64_t* clears, uint64_t* wheel_bytes);

@@ -1,7 +1,7 @@
 """Small fixed workloads for profiling the kernels with ncu.
 
-    python -m voss_gb300.profile_case sieve A B [launches]
-    python -m voss_gb300.profile_case goldbach N [launches]
+    python profile_case.py sieve A B [launches]
+    python profile_case.py goldbach N [launches]
 
 Each case builds a launch plan, runs it once untimed, then launches it the
 given number of times (default 2) on one stream and prints the result, so an
@@ -10,11 +10,14 @@ ncu capture can pick the launches it wants with -k / -s / -c.
 from __future__ import annotations
 
 import sys
+from pathlib import Path
+
+sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 
 def main(argv):
     import torch
-    from .plan import GoldbachPlan, SievePlan
+    from voss_gb300.plan import GoldbachPlan, SievePlan
     kind = argv[0]
     stream = torch.cuda.Stream()
     if kind == "sieve":

@@ -142,6 +142,52 @@ def test_offset_1e12_split_merge_and_known_count(vg):
     assert m.gap_hist_full == whole.gap_hist_full
 
 
+def _production_plan(vg):
+    """The library's own per-range tuning (segment size, tier split and
+    bucket lists from the compiled-in table), as a caller gets it."""
+    cfg = vg.primes.get_config()
+    assert cfg["auto_tune"] == 1 and cfg["bucket_cap_pct"] == 100, cfg
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("a,b", [(10**12, 10**12 + 10**10),          # [1e12, 1e12 + 1e10)
+                                 (10**14, 10**14 + 10**9),           # [1e14, 1e14 + 1e9)
+                                 (10**13, 10**13 + 10**10)])         # a 1e10 window above 1e13
+def test_high_offset_ranges_whole_vs_oracle(vg, oracle_lib, a, b):
+    """The high-offset ranges whole, under the production plan (bucket lists
+    on): every output and all 1025 histogram bins against the oracle."""
+    _production_plan(vg)
+    assert_range_equal(vg.range_stats(a, b, full=True), oracle_lib.range_stats(a, b), (a, b))
+
+
+def test_export_csv(vg, tmp_path):
+    """voss_primes_ctx_export_csv writes the reference's three files
+    (library/src/io/csv.cpp:41-112): names, headers and values as the
+    Context's own queries give them."""
+    import csv
+    for N in (10**6, 10**12):
+        prefix = str(tmp_path / ("run%d" % N))
+        with vg.Context(N) as ctx:
+            files = ctx.export_csv(prefix)
+            cb, st, gaps = ctx.chebyshev(), ctx.statistics(), ctx.large_gaps()
+        assert files == [prefix + "_chebyshev.csv", prefix + "_large_gaps.csv", prefix + "_stats.csv"]
+        rows = list(csv.reader(open(files[0])))
+        assert rows == [["pi_4_1", "pi_4_3", "difference"],
+                        [str(cb.pi_4_1), str(cb.pi_4_3), str(cb.pi_4_3 - cb.pi_4_1)]]
+        rows = list(csv.reader(open(files[1])))
+        assert rows[0] == ["position", "gap"]
+        assert [(int(x), int(y)) for x, y in rows[1:]] == [(g.position, g.gap) for g in gaps]
+        text = open(files[2]).read()
+        assert text == ("metric,value\nmean_gap,%.6f\nstd_dev,%.6f\nskewness,%.6f\nkurtosis,%.6f\n"
+                        "total_gaps,%d\n" % (st.mean_gap, st.std_dev, st.skewness, st.kurtosis, st.total_gaps))
+        if N == 10**6:
+            assert (cb.pi_4_1, cb.pi_4_3) == (39175, 39322) and len(rows) == 1 and st.total_gaps == 78497
+        else:
+            # the reference's 11 gaps >= 500 below 10^12, largest first (test_primes.py:438-458)
+            assert len(gaps) == 11 and (gaps[0].gap, gaps[0].position) == (540, 738832928467)
+            assert st.total_gaps == 37607912018 - 1
+
+
 def test_offset_1e14_subwindows_vs_oracle(vg, oracle_lib):
     a = 10**14
     for off in (0, 123456789, 5 * 10**8, 10**9 - 3 * 10**6):

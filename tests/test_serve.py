@@ -39,6 +39,45 @@ def test_served_equals_alone(vg, oracle_lib):
             assert got.max_gap == orc["max_gap"] and got.twins == int(orc["hist"][1])
 
 
+def _assert_matches_oracle(r, got, orc):
+    """A served answer against the oracle's statistics of [r.a, r.b): counts,
+    Chebyshev classes and first/last prime for every op; for gap ops also
+    the whole public histogram (bins 0..200 and the bin of gaps above 400),
+    twins/cousins/sexy, the largest gap and its start, the gap count and the
+    gaps >= 500; count-only ops carry no gap outputs."""
+    from voss_gb300.serve import GAP_OPS
+    h = orc["hist"]
+    assert (got.count, got.first_prime, got.last_prime) == (orc["count"], orc["first"], orc["last"]), r
+    assert (got.pi_4_1, got.pi_4_3, got.pi_3_1, got.pi_3_2) == (
+        orc["pi_4_1"], orc["pi_4_3"], orc["pi_3_1"], orc["pi_3_2"]), r
+    if r.op in GAP_OPS:
+        assert got.gap_hist[:201] == [int(x) for x in h[:201]], r
+        assert got.gap_hist[201] == int(h[201:].sum()), r
+        assert (got.twins, got.cousins, got.sexy) == (int(h[1]), int(h[2]), int(h[3])), r
+        assert (got.max_gap, got.max_gap_start, got.num_gaps) == (
+            orc["max_gap"], orc["max_gap_start"], orc["num_gaps"]), r
+        assert got.large_gaps == int(h[250:].sum()), r
+    else:
+        assert got.max_gap == 0 and got.twins == 0 and not any(got.gap_hist), r
+
+
+@pytest.mark.gpu
+@pytest.mark.slow
+def test_served_mix_vs_oracle(vg, oracle_lib):
+    """500 requests of the serving mix at its real sizes (starts up to 10^13,
+    widths up to 10^10, all four ops), served with continuous batching and
+    shared pieces: every answer against the oracle."""
+    from voss_gb300.serve import Server, run_served, serving_mix
+    reqs = serving_mix(500, seed=20261204)
+    assert max(r.b - r.a for r in reqs) > 5 * 10**9 and max(r.a for r in reqs) > 10**12
+    with Server() as srv:
+        res, lat, wall = run_served(srv, reqs)
+        m = srv.metrics()
+    assert m["completed"] == len(reqs)
+    for r, got in zip(reqs, res):
+        _assert_matches_oracle(r, got, oracle_lib.range_stats(r.a, r.b))
+
+
 @pytest.mark.gpu
 def test_poisson_arrivals_and_admission_limits(vg):
     from voss_gb300.serve import Server, run_served, same_answer, serving_mix

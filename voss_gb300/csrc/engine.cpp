@@ -699,10 +699,12 @@ uint64_t Plan::wheel_bytes() const {
 }
 
 uint64_t Plan::algorithmic_clears() const {
-  // The candidate clears of Eratosthenes by the primes p >= 37 with
-  // p*p < b: for each such p and class o, the k in [k_lo, k_hi) with
-  // k = R (mod p) and 30k + W30[o] >= p*p.  The table primes (>= 61) are
-  // cleared by the marking tiers, 37..59 by the presieve tiles; both count.
+  // The algorithmic work of the sieve: the candidate clears of Eratosthenes
+  // by every prime 17 < p with p*p < b (7..17 being the wheel-and-pattern
+  // primes every wheel-30 sieve presieves): for each such p and class o, the
+  // k in [k_lo, k_hi) with k = R (mod p) and 30k + W30[o] >= p*p.  The table
+  // primes (>= 61) are cleared by the marking tiers, 19..59 by the presieve
+  // tiles; the count is the same whichever does the work.
   const Engine& E = *eng;
   uint64_t total = 0;
   auto clears = [&](const ReqDesc& r, uint64_t p) {
@@ -716,7 +718,7 @@ uint64_t Plan::algorithmic_clears() const {
     }
   };
   for (const ReqDesc& r : host_reqs) {
-    for (uint64_t p : {37ull, 41ull, 43ull, 47ull, 53ull, 59ull})
+    for (uint64_t p : {19ull, 23ull, 29ull, 31ull, 37ull, 41ull, 43ull, 47ull, 53ull, 59ull})
       if (p * p < r.b) clears(r, p);
     for (uint32_t i = 0; i < r.nprimes; ++i) clears(r, E.hP[i]);
   }

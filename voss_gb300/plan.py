@@ -97,3 +97,11 @@ def smem_peak() -> dict:
     a, b = ctypes.c_double(), ctypes.c_double()
     _capi._check(_capi._lib.voss_gb300_smem_peak(ctypes.byref(a), ctypes.byref(b)), {})
     return {"ldst_gbs": a.value, "atomic_gbs": b.value}
+
+
+def device_info() -> dict:
+    """Name and SM count of the device the library runs on."""
+    name = ctypes.create_string_buffer(256)
+    sms = ctypes.c_uint32()
+    _capi._check(_capi._lib.voss_gb300_device_info(name, 256, ctypes.byref(sms)), {})
+    return {"name": name.value.decode(), "sm_count": sms.value}
