@@ -98,7 +98,7 @@ int voss_primes_range_stats_noalloc(uint64_t a, uint64_t b, voss_range_stats_t* 
                                     void* stream);
 
 /* Tunables of the segmented sieve.  seg_bytes: shared-memory segment in
- * bytes (30 integers each), a multiple of 128, at most 226944.  threads: CTA
+ * bytes (30 integers each), a multiple of 128, at most 222848.  threads: CTA
  * size (multiple of 32, <= 1024).  tier_split: primes below it are marked a
  * warp per prime, primes from it on four primes per warp.  ctas_per_sm: resident
  * CTAs per SM used to size the persistent grid.  Zero fields keep the

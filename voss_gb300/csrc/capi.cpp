@@ -688,8 +688,8 @@ extern "C" int voss_gb300_get_config(voss_gb300_config_t* out) {
 
 extern "C" int voss_gb300_set_config(const voss_gb300_config_t* c) {
   if (!c) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
-  if (c->seg_bytes && (c->seg_bytes % 128 || c->seg_bytes < 1024 || c->seg_bytes > 226944)) {
-    set_err("seg_bytes must be a multiple of 128 in [1024, 226944]");
+  if (c->seg_bytes && (c->seg_bytes % 128 || c->seg_bytes < 1024 || c->seg_bytes > vg::kMaxSegBytes)) {
+    set_err("seg_bytes must be a multiple of 128 in [1024, " + std::to_string(vg::kMaxSegBytes) + "]");
     return VOSS_ERR_INVALID_ARG;
   }
   if (c->threads && (c->threads % 32 || c->threads > 1024 || c->threads < 64)) {
@@ -723,9 +723,10 @@ extern "C" int voss_gb300_set_config(const voss_gb300_config_t* c) {
 extern "C" int voss_gb300_set_tuning(uint32_t n, const voss_gb300_tune_entry_t* e) {
   if (n && !e) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
   for (uint32_t i = 0; i < n; ++i)
-    if (e[i].seg_bytes < 1024 || e[i].seg_bytes > 226944 || e[i].seg_bytes % 128 ||
+    if (e[i].seg_bytes < 1024 || e[i].seg_bytes > vg::kMaxSegBytes || e[i].seg_bytes % 128 ||
         e[i].tier_split < kMinTierSplit) {
-      set_err("tuning entry out of range (seg_bytes in [1024, 226944], multiple of 128; tier_split >= 37)");
+      set_err("tuning entry out of range (seg_bytes in [1024, " + std::to_string(vg::kMaxSegBytes) +
+              "], multiple of 128; tier_split >= 37)");
       return VOSS_ERR_INVALID_ARG;
     }
   return guarded([&] {

@@ -68,8 +68,6 @@ HostPinned::~HostPinned() {
 }
 
 static const uint32_t kW30[8] = {1, 7, 11, 13, 17, 19, 23, 29};
-// Largest segment any config may use; tiles are extended by this much.
-static const uint32_t kMaxSegBytes = 226944;
 
 static int64_t inverse_mod(int64_t a, int64_t m) {
   int64_t t = 0, nt = 1, r = m, nr = a % m;
@@ -104,7 +102,9 @@ void Engine::init() {
   cudaDeviceProp prop;
   check_cuda(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
   sm_count = (uint32_t)prop.multiProcessorCount;
-  max_smem_optin = prop.sharedMemPerBlockOptin;
+  // room for the sieve kernel's dynamic shared memory: the opt-in limit
+  // less the kernel's own static shared memory
+  max_smem_optin = prop.sharedMemPerBlockOptin - sieve_static_smem_bytes();
   name = prop.name;
   check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
   // Fit the default segment into what this device offers.

@@ -52,7 +52,7 @@ struct HostPinned {
 };
 
 struct Config {
-  uint32_t seg_bytes = 226944;    // the largest that fits with the histograms (227 KB per CTA)
+  uint32_t seg_bytes = kMaxSegBytes;    // the largest that fits (227 KB of shared memory per CTA)
   uint32_t threads = 1024;
   uint32_t tier_split = 6144;    // primes below: a warp per prime; above: 4 per warp
   uint32_t ctas_per_sm = 1;
@@ -201,7 +201,7 @@ class Engine {
   std::mutex mu;     // one caller at a time per device
   int device = 0;
   uint32_t sm_count = 0;
-  size_t max_smem_optin = 0;
+  size_t max_smem_optin = 0;    // dynamic shared memory the sieve kernel may ask for
   std::string name;
   cudaStream_t stream = nullptr;
   Config cfg;
@@ -253,6 +253,7 @@ void to_public(const ReqResult& r, uint64_t a, uint64_t b, voss_range_stats_t* o
 
 // Launchers defined in sieve.cu.
 size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads);
+size_t sieve_static_smem_bytes();      // the sieve kernel's static shared memory
 cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads,
                          cudaStream_t stream);
 cudaError_t launch_bucket_fill(const FillParams& fp, uint32_t grid, cudaStream_t stream);

@@ -210,6 +210,7 @@ sieve_segments_kernel(const SieveParams prm) {
   uint32_t* seg = smem;
   uint32_t* shist = seg + (prm.seg_bytes >> 2);
   WarpRec* wrec = reinterpret_cast<WarpRec*>(shist + kSmemHistCopies * kSmemStride);
+  uint4* btab = reinterpret_cast<uint4*>(wrec + kMaxThreads / 32);   // the gap scan's byte table
 
   // the segment in hand, s_item[cur], and the next one, s_item[cur ^ 1],
   // claimed and looked up by warp 0 while the others mark (so no thread
@@ -223,6 +224,10 @@ sieve_segments_kernel(const SieveParams prm) {
 
   for (uint32_t i = tid; i < kSmemHistCopies * kSmemStride; i += nthr) shist[i] = 0;
   if (tid < 32) s_vtab[tid] = 30u * (tid >> 3) + w30(tid & 7u);
+  for (uint32_t i = tid; i < kByteTabEntries; i += nthr) {
+    const uint64_t e = byte_gap_entry(i, false), od = byte_gap_entry(i, true);
+    btab[i] = make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)od, (uint32_t)(od >> 32));
+  }
   if (tid == 0) s_ctr = 0;
   int cur_req = -1;
 
@@ -432,43 +437,103 @@ sieve_segments_kernel(const SieveParams prm) {
       uint32_t first1 = 0, last1 = 0, cnt = 0, c41 = 0, c31 = 0, maxg = 0, maxgs = 0;
       const bool gaps = (S.rflags & kReqGaps) != 0;
       if (gaps) {
-        // the run's first prime opens no gap: it is taken before the main
-        // loop, which then records a gap for every prime it meets
-        uint32_t wi = wbeg, pv = 0;
-        bool have = false;
-        for (; wi < wend && !have; ++wi) {
-          uint32_t w = seg[wi];
-          if (!w) continue;
-          cnt += __popc(w);
-          c41 += __popc(w & m41);
-          c31 += __popc(w & 0x2B2B2B2Bu);
-          const uint32_t vb = 120u * wi;
-          pv = vb + s_vtab[__ffs(w) - 1];
-          w &= w - 1u;
-          first1 = pv + 1u;
-          have = true;
-          while (w) {
-            const uint32_t v = vb + s_vtab[__ffs(w) - 1];
-            w &= w - 1u;
-            record_gap(sk, pv, v, maxg, maxgs);
-            pv = v;
+        // Byte by byte, four fixed steps per word, so the lanes of a warp
+        // stay in step whatever their primes: the gaps inside a wheel byte
+        // (2..28) come from the byte table and are summed in packed 8-bit
+        // counters (accE: gap/2 - 1 even, accO: odd), flushed warp-reduced
+        // into the shared histogram every kFlushWords words; the gap into a
+        // byte from the previous prime goes to the histogram directly, and
+        // to the rare path when it may be a new largest gap, a large gap or
+        // beyond the shared bins.  The run's first prime arrives as a gap
+        // from kNoPrev, which the rare path takes as "no gap, first prime".
+        constexpr uint32_t kNoPrev = 0x80000000u;
+        constexpr uint32_t kFlushWords = 15;      // 15 words * 4 bytes * 4 gaps of one size < 256
+        uint64_t accE = 0, accO = 0;
+        uint32_t pv = kNoPrev, thr = 0;
+        const uint32_t nsteps = run;              // the same for every lane
+        for (uint32_t i = 0; i < nsteps; ++i) {
+          const uint32_t wi = wbeg + i;
+          const uint32_t w = wi < wend ? seg[wi] : 0u;
+          if (w) {
+            cnt += __popc(w);
+            c41 += __popc(w & m41);
+            c31 += __popc(w & 0x2B2B2B2Bu);
+            const uint32_t vb = 120u * wi;
+#pragma unroll
+            for (uint32_t b = 0; b < 4; ++b) {
+              const uint32_t x = (w >> (8u * b)) & 0xFFu;
+              if (x) {
+                const uint4 t = btab[x];
+                accE += ((uint64_t)t.y << 32) | t.x;
+                accO += ((uint64_t)t.w << 32) | t.z;
+                const uint32_t v = vb + 30u * b + (t.y >> 24);
+                const uint32_t g = v - pv;
+                if (g <= thr) {
+                  atomicAdd(sk.shist + (g >> 1), 1u);
+                } else if (g & kNoPrev) {
+                  first1 = v + 1u;                  // the run's first prime
+                } else {
+                  const uint32_t bin = g >> 1;
+                  if (bin < (uint32_t)kSmemBins) atomicAdd(sk.shist + bin, 1u);
+                  else atomicAdd(&sk.acc->hist[bin < (uint32_t)kHistBins ? bin : kHistBins - 1], 1ull);
+                  if (g > maxg) { maxg = g; maxgs = pv; }
+                  if (g >= kLargeGap) {
+                    const unsigned idx = atomicAdd(sk.n_large, 1u);
+                    if (idx < sk.cap) {
+                      LargeGapRec r; r.pos = sk.base + v; r.gap = g; r.req = sk.req;
+                      sk.large[idx] = r;
+                    }
+                  }
+                  thr = min(maxg, kLargeGap - 1u);
+                }
+                pv = vb + 30u * b + (t.w >> 24);
+              }
+            }
+          }
+          if ((i + 1u) % kFlushWords == 0u || i + 1u == nsteps) {
+            // 16-bit pairs of the 8-bit counters, summed over the warp; lane
+            // k < 7 adds pair k (bins 2k+1, 2k+3 from accE; k >= 4 accO)
+            const uint32_t eL = (uint32_t)accE, eH = (uint32_t)(accE >> 32);
+            const uint32_t oL = (uint32_t)accO, oH = (uint32_t)(accO >> 32);
+            const uint32_t q0 = __reduce_add_sync(0xFFFFFFFFu, __byte_perm(eL, 0u, 0x5150));   // bins 1, 3
+            const uint32_t q1 = __reduce_add_sync(0xFFFFFFFFu, __byte_perm(eL, 0u, 0x5352));   // bins 5, 7
+            const uint32_t q2 = __reduce_add_sync(0xFFFFFFFFu, __byte_perm(eH, 0u, 0x5150));   // bins 9, 11
+            const uint32_t q3 = __reduce_add_sync(0xFFFFFFFFu, __byte_perm(eH, 0u, 0x4442));   // bin 13
+            const uint32_t q4 = __reduce_add_sync(0xFFFFFFFFu, __byte_perm(oL, 0u, 0x5150));   // bins 2, 4
+            const uint32_t q5 = __reduce_add_sync(0xFFFFFFFFu, __byte_perm(oL, 0u, 0x5352));   // bins 6, 8
+            const uint32_t q6 = __reduce_add_sync(0xFFFFFFFFu, __byte_perm(oH, 0u, 0x5150));   // bins 10, 12
+            const uint32_t q7 = __reduce_add_sync(0xFFFFFFFFu, __byte_perm(oH, 0u, 0x4442));   // bin 14
+            accE = 0;
+            accO = 0;
+            if (lane < 8u) {
+              const uint32_t q = lane == 0 ? q0 : lane == 1 ? q1 : lane == 2 ? q2 : lane == 3 ? q3
+                               : lane == 4 ? q4 : lane == 5 ? q5 : lane == 6 ? q6 : q7;
+              // pair k of accE holds bins 4k'+1.. : lane 0 -> 1,3; 1 -> 5,7; 2 -> 9,11; 3 -> 13
+              // accO: lane 4 -> 2,4; 5 -> 6,8; 6 -> 10,12; 7 -> 14
+              const uint32_t b0 = lane < 4u ? 4u * lane + 1u : 4u * (lane - 4u) + 2u;
+              if (q & 0xFFFFu) atomicAdd(sk.shist + b0, q & 0xFFFFu);
+              if (q >> 16) atomicAdd(sk.shist + b0 + 2u, q >> 16);
+            }
           }
         }
-        for (; wi < wend; ++wi) {
-          uint32_t w = seg[wi];
-          if (!w) continue;
-          cnt += __popc(w);
-          c41 += __popc(w & m41);
-          c31 += __popc(w & 0x2B2B2B2Bu);
-          const uint32_t vb = 120u * wi;
-          do {
-            const uint32_t v = vb + s_vtab[__ffs(w) - 1];
-            w &= w - 1u;
-            record_gap(sk, pv, v, maxg, maxgs);
-            pv = v;
-          } while (w);
+        // A largest gap inside a byte (at most 28) is not tracked above:
+        // where no gap between bytes exceeds 28, the run is walked prime by
+        // prime for its exact largest gap (the earliest one on ties).
+        if (first1 && maxg <= 28u) {
+          maxg = 0; maxgs = 0;
+          uint32_t q = first1 - 1u;
+          for (uint32_t wi = wbeg; wi < wend; ++wi) {
+            uint32_t w = seg[wi];
+            const uint32_t vb = 120u * wi;
+            while (w) {
+              const uint32_t v = vb + s_vtab[__ffs(w) - 1];
+              w &= w - 1u;
+              if (v - q > maxg) { maxg = v - q; maxgs = q; }
+              q = v;
+            }
+          }
         }
-        last1 = have ? pv + 1u : 0u;
+        last1 = first1 ? pv + 1u : 0u;
       } else {
         for (uint32_t wi = wbeg; wi < wend; ++wi) {
           const uint32_t w = seg[wi];
@@ -841,9 +906,15 @@ __global__ void zero_kernel(ZeroSpan z0, ZeroSpan z1, ZeroSpan z2) {
 // ---------------------------------------------------------------------------
 // host-side launchers (called by the engine)
 // ---------------------------------------------------------------------------
-size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads) {
+size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t /*threads*/) {
+  // segment, histogram copies, warp records (room for 32 warps), byte table
   return (size_t)seg_bytes + sizeof(uint32_t) * kSmemHistCopies * kSmemStride +
-         sizeof(WarpRec) * (threads / 32);
+         sizeof(WarpRec) * (kMaxThreads / 32) + sizeof(uint4) * kByteTabEntries;
+}
+
+size_t sieve_static_smem_bytes() {
+  cudaFuncAttributes a{};
+  return cudaFuncGetAttributes(&a, sieve_segments_kernel) == cudaSuccess ? a.sharedSizeBytes : 1024;
 }
 
 cudaError_t launch_sieve(const SieveParams& prm, uint32_t grid, uint32_t threads,

@@ -17,6 +17,34 @@ constexpr int kSmemBins = 256;        // bins kept in shared memory (gap < 512)
 constexpr int kSmemHistCopies = 4;    // one copy per 8 warps
 constexpr int kSmemStride = kSmemBins + 4;   // + the overflow bin, padded
 constexpr uint32_t kLargeGap = 500;   // the reference's large-gap threshold
+// Largest segment: what one CTA's 227 KB of shared memory holds beside the
+// histogram copies, the warp records and the byte table of the gap scan.
+constexpr uint32_t kMaxSegBytes = 222848;
+// The gap scan's byte table: for each value of a wheel byte, the gaps between
+// its consecutive candidates (30k + W30[o] for its set bits o) counted per
+// gap/2 - 1 = j (j = 0..13, gaps 2..28; at most 4 of one size) in 8-bit
+// fields -- even j in .x/.y
+// byte j/2, odd j in .z/.w byte (j-1)/2 -- with W30 of the byte's lowest set
+// bit in the top byte of .y and of its highest in the top byte of .w.
+constexpr uint32_t kByteTabEntries = 256;
+constexpr uint32_t kInByteBins = 14;
+__host__ __device__ constexpr uint64_t byte_gap_entry(uint32_t x, bool odd) {
+  uint64_t e = 0;
+  int prev = -1, lo = -1, hi = -1;
+  for (int o = 0; o < 8; ++o) {
+    if (!((x >> o) & 1u)) continue;
+    const int v = (int)((kW30Packed >> (8 * o)) & 0xFFu);
+    if (lo < 0) lo = v;
+    hi = v;
+    if (prev >= 0) {
+      const int j = (v - prev) / 2 - 1;
+      if ((j & 1) == (odd ? 1 : 0)) e += 1ull << (8 * (j >> 1));
+    }
+    prev = v;
+  }
+  const int top = odd ? hi : lo;
+  return e | ((uint64_t)(top < 0 ? 0 : top) << 56);
+}
 // Presieve tiles: the wheel bytes with the multiples of a few small primes
 // cleared are periodic, with period the product of those primes (in bytes).
 // Four tiles cover the primes 7..59.

@@ -15,7 +15,7 @@ from typing import List, Sequence
 from .primes import RangeStats
 
 # Shard boundaries fall on whole segments of the largest default segment.
-ALIGN = 30 * 226944
+ALIGN = 30 * 222848
 LARGE_GAP = 500
 
 
