@@ -400,6 +400,27 @@ def test_bucket_lists_vs_oracle(vg, oracle_lib):
             vg.primes.set_config(**base)
 
 
+def test_windowed_bucket_lists_vs_oracle(vg, oracle_lib):
+    """A range of more segments than one set of bucket lists holds is sieved in
+    windows, each window filling the same list memory afresh: small segments
+    force three windows; the production tuning gives two just below 10^13."""
+    a, b = 10**13 + 12345, 10**13 + 12345 + 5 * 10**9
+    want = oracle_lib.range_stats(a, b)
+    base = _with_config(vg, seg_bytes=16384, tier_split=512, bucket_split=65536, auto_tune=0)
+    try:
+        from voss_gb300.plan import SievePlan
+        plan = SievePlan([(a, b)])
+        info = plan.info()
+        plan.close()
+        assert info["segments"] > 2 * 4096, info
+        assert info["kernels_per_run"] >= 2 + 2 * 3, info      # a fill and a sieve per window
+        assert_range_equal(vg.range_stats(a, b, full=True), want, "windows of 16 KiB segments")
+    finally:
+        vg.primes.set_config(**base)
+    a, b = 10**13 - 3 * 10**10, 10**13
+    assert_range_equal(vg.range_stats(a, b, full=True), oracle_lib.range_stats(a, b), "production windows")
+
+
 def test_bucket_overflow_falls_back(vg, oracle_lib):
     """Lists far too small for their hits: the run repeats without lists."""
     a, b = 10**14, 10**14 + 3 * 10**7

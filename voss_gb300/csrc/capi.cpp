@@ -808,7 +808,7 @@ extern "C" int voss_gb300_plan_info(voss_gb300_plan* p, uint64_t* total_segments
     if (total_segments) *total_segments = p->plan.total_segs;
     if (grid) *grid = p->plan.grid;
     if (kernels_per_run)
-      *kernels_per_run = p->plan.nreq ? vg::Plan::kKernels + (p->plan.nfill ? 1u : 0u) : 0;
+      *kernels_per_run = p->plan.kernels_per_run();
     if (smem_bytes) *smem_bytes = (uint32_t)vg::sieve_smem_bytes(p->plan.seg_max, p->plan.threads);
     if (clears) *clears = p->plan.algorithmic_clears();
     if (wheel_bytes) *wheel_bytes = p->plan.wheel_bytes();

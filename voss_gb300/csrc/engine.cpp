@@ -247,7 +247,7 @@ BucketPlan Engine::bucket_plan(const Config& c, uint64_t b, uint32_t nprimes, ui
   // above the segment, a request of several segments (one fill pass replaces
   // a setup per prime per segment), few enough segments for the fill
   // kernel's shared counts.
-  if (!c.bucket_split || nseg < 2 || nseg > kMaxBucketSegs || b < 2) return bp;
+  if (!c.bucket_split || nseg < 2 || b < 2) return bp;
   const uint32_t from = std::max<uint32_t>(c.bucket_split, seg_bytes);
   const uint32_t idx = index_of(from);
   if (idx >= nprimes) return bp;
@@ -300,8 +300,21 @@ uint64_t Plan::list_bytes_for(uint64_t a, uint64_t b) const {
   const Config c = E.tuned_for(a, b, batch_mode);
   const uint64_t bytes = (b + 29) / 30 - a / 30;
   const uint64_t nseg = (bytes + c.seg_bytes - 1) / c.seg_bytes;
+  // plans of many requests hold every request's lists at once (no windows)
+  if (nseg > kMaxBucketSegs) return 0;
   const BucketPlan bp = E.bucket_plan(c, b, E.primes_below_sq(b), nseg, c.seg_bytes);
   return bp.cap ? 4ull * bp.cap * nseg : 0;
+}
+
+uint32_t Plan::kernels_per_run() const {
+  if (!nreq) return 0;
+  const uint32_t fixed = kKernels + ((cap_req ? cap_out : nout) ? 1u : 0u);
+  if (!wins.empty()) {
+    uint32_t k = fixed - 1u;                 // zero + finalize (+ combine)
+    for (const Window& W : wins) k += 1u + (W.fill_hi > W.fill_lo ? 1u : 0u);
+    return k;
+  }
+  return fixed + ((cap_req ? cap_fill : nfill) ? 1u : 0u);
 }
 
 uint32_t Plan::fill_grid_max() const {
@@ -442,6 +455,7 @@ void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint3
   host_reqs.resize(n);
   order.resize(n);
   host_fills.clear();
+  wins.clear();
   uint64_t base = 0, bbase = 0;
   for (uint32_t i = 0; i < n; ++i) {
     ReqDesc& r = host_reqs[i];
@@ -452,29 +466,39 @@ void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint3
     r.bucket_cap = 0;
     order[i] = items[i].idx;
     base += r.nseg;
-    if (allow_buckets && r.nseg && !(fl & kFlagBitmap)) {
+    // a lone request of a plan without fixed capacity may be windowed
+    const bool windowed = !cap_req && n == 1 && r.nseg > kMaxBucketSegs;
+    if (allow_buckets && r.nseg && !(fl & kFlagBitmap) && (windowed || r.nseg <= kMaxBucketSegs)) {
       const Config c = E.tuned_for(r.a, r.b, many);
       const BucketPlan bp = E.bucket_plan(c, r.b, r.nprimes, r.nseg, r.seg_bytes);
-      const uint64_t need = (uint64_t)bp.cap * r.nseg;
+      const uint64_t wsegs = std::min<uint64_t>(r.nseg, kMaxBucketSegs);   // segments per window
+      const uint64_t need = (uint64_t)bp.cap * wsegs;
       if (bp.cap) {
-        // fill items: runs of kFillPrimes primes; a run's hits (8 per p
-        // bytes per prime) split over segment ranges so that every item
-        // carries at most about kFillHits hits: items balance, and the list
-        // blocks that the resident fill CTAs are writing at any time (their
-        // items' entries) stay well inside L2, so lines leave it complete
-        const uint32_t nseg = (uint32_t)r.nseg;
-        const double per = 8.0 * (double)(r.k_hi - r.k_lo);
-        const double target = kFillHits;
+        // fill items, per window: runs of kFillPrimes primes; a run's hits
+        // (8 per p bytes per prime) split over segment ranges so that every
+        // item carries at most about kFillHits hits: items balance, and the
+        // list blocks that the resident fill CTAs are writing at any time
+        // (their items' entries) stay well inside L2, so lines leave it
+        // complete
         item_buf.clear();
-        for (uint32_t p0 = bp.bucket_idx; p0 < r.nprimes; p0 += kFillPrimes) {
-          const uint32_t p1 = std::min<uint32_t>(p0 + kFillPrimes, r.nprimes);
-          const double hits = per * (E.hInvPrefix[p1] - E.hInvPrefix[p0]);
-          const uint32_t pieces = (uint32_t)std::min<double>(nseg, std::max(1.0, std::ceil(hits / target)));
-          for (uint32_t j = 0; j < pieces; ++j) {
-            const uint32_t g0 = (uint32_t)((uint64_t)nseg * j / pieces);
-            const uint32_t g1 = (uint32_t)((uint64_t)nseg * (j + 1) / pieces);
-            item_buf.push_back(FillItem{i, p0, p1, g0 | (g1 << 16)});
+        std::vector<Window> rw;
+        for (uint64_t w0 = 0; w0 < r.nseg; w0 += wsegs) {
+          const uint32_t nseg = (uint32_t)std::min<uint64_t>(wsegs, r.nseg - w0);
+          const uint64_t kw = r.k_lo + w0 * r.seg_bytes;
+          const double per = 8.0 * (double)std::min<uint64_t>(r.k_hi - kw, (uint64_t)nseg * r.seg_bytes);
+          const uint32_t f0 = (uint32_t)item_buf.size();
+          for (uint32_t p0 = bp.bucket_idx; p0 < r.nprimes; p0 += kFillPrimes) {
+            const uint32_t p1 = std::min<uint32_t>(p0 + kFillPrimes, r.nprimes);
+            const double hits = per * (E.hInvPrefix[p1] - E.hInvPrefix[p0]);
+            const uint32_t pieces = (uint32_t)std::min<double>(nseg, std::max(1.0, std::ceil(hits / kFillHits)));
+            for (uint32_t j = 0; j < pieces; ++j) {
+              const uint32_t g0 = (uint32_t)((uint64_t)nseg * j / pieces);
+              const uint32_t g1 = (uint32_t)((uint64_t)nseg * (j + 1) / pieces);
+              item_buf.push_back(FillItem{i, p0, p1, g0 | (g1 << 16)});
+            }
           }
+          rw.push_back(Window{r.seg_base + w0, r.seg_base + w0 + nseg, f0, (uint32_t)item_buf.size(),
+                              (uint32_t)w0});
         }
         const bool fits = !cap_req || (bbase + need <= cap_bucket && host_fills.size() + item_buf.size() <= cap_fill);
         if (fits) {
@@ -483,6 +507,7 @@ void Plan::load_requests(uint32_t n, const uint64_t* a, const uint64_t* b, uint3
           r.bucket_base = bbase;
           bbase += need;
           host_fills.insert(host_fills.end(), item_buf.begin(), item_buf.end());
+          if (windowed) wins = std::move(rw);
         }
       }
     }
@@ -617,21 +642,42 @@ void Plan::run_device(cudaStream_t s) {
              "zero_kernel");
   // the sieve's timed span covers the bucket fill that feeds it
   if (timed) check_cuda(cudaEventRecord(ev[0], s), "event");
-  if (cap_req ? cap_fill : nfill) {
-    FillParams fp;
-    fp.reqs = dreqs();
-    fp.hdr = hdr.as<BatchHdr>();
-    fp.items = fills.as<FillItem>();
-    fp.P = prm.P;
-    fp.M = prm.M;
-    fp.R = prm.R;
-    fp.bucket = bucket.as<uint32_t>();
-    fp.bcount = bcount.as<uint32_t>();
-    fp.overflow = &dctl()->overflow;
-    const uint32_t fgrid = cap_req ? fill_grid_max() : std::min<uint32_t>(nfill, fill_grid_max());
-    check_cuda(launch_bucket_fill(fp, fgrid, s), "bucket_fill_kernel");
+  FillParams fp{};
+  fp.reqs = dreqs();
+  fp.hdr = hdr.as<BatchHdr>();
+  fp.items = fills.as<FillItem>();
+  fp.P = prm.P;
+  fp.M = prm.M;
+  fp.R = prm.R;
+  fp.bucket = bucket.as<uint32_t>();
+  fp.bcount = bcount.as<uint32_t>();
+  fp.overflow = &dctl()->overflow;
+  if (wins.empty()) {
+    if (cap_req ? cap_fill : nfill) {
+      const uint32_t fgrid = cap_req ? fill_grid_max() : std::min<uint32_t>(nfill, fill_grid_max());
+      check_cuda(launch_bucket_fill(fp, fgrid, s), "bucket_fill_kernel");
+    }
+    check_cuda(launch_sieve(prm, grid, threads, s), "sieve_segments_kernel");
+  } else {
+    // one window at a time: fill its lists, then sieve its segments; each
+    // sieve launch counts its own work queue from zero
+    const uint64_t gcap = (uint64_t)eng->sm_count * eng->cfg.ctas_per_sm;
+    for (size_t w = 0; w < wins.size(); ++w) {
+      const Window& W = wins[w];
+      if (w) check_cuda(cudaMemsetAsync(&dctl()->queue, 0, sizeof(unsigned long long), s), "reset work queue");
+      fp.items = fills.as<FillItem>() + W.fill_lo;
+      fp.nitems = W.fill_hi - W.fill_lo;
+      fp.seg0 = W.seg0;
+      if (fp.nitems)
+        check_cuda(launch_bucket_fill(fp, std::min<uint32_t>(fp.nitems, fill_grid_max()), s), "bucket_fill_kernel");
+      SieveParams wp = prm;
+      wp.item_lo = W.item_lo;
+      wp.item_hi = W.item_hi;
+      wp.list_seg0 = W.seg0;
+      check_cuda(launch_sieve(wp, (uint32_t)std::min<uint64_t>(W.item_hi - W.item_lo, gcap), threads, s),
+                 "sieve_segments_kernel");
+    }
   }
-  check_cuda(launch_sieve(prm, grid, threads, s), "sieve_segments_kernel");
   if (timed) check_cuda(cudaEventRecord(ev[1], s), "event");
   check_cuda(launch_finalize(dreqs(), hdr.as<BatchHdr>(), segs.as<SegRec>(),
                              acc.as<ReqAccum>(), large.as<LargeGapRec>(),

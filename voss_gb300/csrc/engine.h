@@ -109,6 +109,17 @@ struct Plan {
   std::vector<uint32_t> atom_rf;
   std::vector<FillItem> host_fills;
   std::vector<FillItem> item_buf;   // one request's fill items, before the capacity check
+  // A lone request of more than kMaxBucketSegs segments with bucket lists
+  // (plans without a fixed capacity only) runs in windows of kMaxBucketSegs
+  // segments: per window a fill of its lists (host_fills[fill_lo, fill_hi),
+  // segments counted from seg0) and a sieve launch over its work items, all
+  // windows reusing one list arena.  Empty: one fill and one sieve launch.
+  struct Window {
+    uint64_t item_lo, item_hi;
+    uint32_t fill_lo, fill_hi;
+    uint32_t seg0;
+  };
+  std::vector<Window> wins;
   HostPinned stage;             // BatchHdr followed by ReqDesc[cap]
   HostPinned host_results;      // ReqResult[] in device order (caller order when shared)
   HostPinned host_flag;         // the overflow flag, copied with the results
@@ -174,6 +185,8 @@ struct Plan {
   bool overflowed() const;
   // resident CTAs of the bucket fill kernel over the whole GPU
   uint32_t fill_grid_max() const;
+  // kernel launches of one run
+  uint32_t kernels_per_run() const;
 };
 
 // Bucket layout of one request: first bucket prime, list capacity per

@@ -144,11 +144,12 @@ __device__ __forceinline__ uint32_t warp_count_leading(uint32_t n, uint32_t lane
 // below its upper end, and its bucket list.  Lane 0 writes d.
 __device__ __noinline__ void claim_item(unsigned long long* queue, const ReqDesc* __restrict__ reqs,
                                         const uint32_t* __restrict__ P, const uint32_t* __restrict__ bcount,
-                                        uint64_t total_segs, uint32_t nreq, SegItem& d, uint32_t lane) {
+                                        uint64_t item_lo, uint64_t item_end, uint64_t list_seg0,
+                                        uint32_t nreq, SegItem& d, uint32_t lane) {
   unsigned long long it = 0;
   if (lane == 0) it = atomicAdd(queue, 1ull);
-  const uint64_t item = __shfl_sync(0xFFFFFFFFu, it, 0);
-  if (item >= total_segs) {
+  const uint64_t item = item_lo + __shfl_sync(0xFFFFFFFFu, it, 0);
+  if (item >= item_end) {
     if (lane == 0) { d.item = item; d.valid = 0; }
     return;
   }
@@ -171,7 +172,7 @@ __device__ __noinline__ void claim_item(unsigned long long* queue, const ReqDesc
     if (R.bucket_idx < a) {
       a = R.bucket_idx;
       d.bcnt = min(bcount[item], R.bucket_cap);
-      d.bbase = R.bucket_base + si * (uint64_t)R.bucket_cap;
+      d.bbase = R.bucket_base + (si - list_seg0) * (uint64_t)R.bucket_cap;
     }
     d.item = item; d.valid = 1;
     d.req = r; d.k0 = k0; d.nbytes = nb; d.np = a;
@@ -232,9 +233,10 @@ sieve_segments_kernel(const SieveParams prm) {
   int cur_req = -1;
 
   const uint64_t total_segs = prm.hdr->total_segs;
+  const uint64_t item_end = prm.item_hi ? min(total_segs, prm.item_hi) : total_segs;
   const uint32_t nreq = prm.hdr->nreq;
   uint32_t cur = 0;
-  if (warp == 0) claim_item(prm.queue, prm.reqs, prm.P, prm.bcount, total_segs, nreq, s_item[0], lane);
+  if (warp == 0) claim_item(prm.queue, prm.reqs, prm.P, prm.bcount, prm.item_lo, item_end, prm.list_seg0, nreq, s_item[0], lane);
   __syncthreads();
   // Three barriers per segment: after the fill, after the marking, before
   // the warps are stitched.  No thread reads the segment after the last one,
@@ -307,7 +309,8 @@ sieve_segments_kernel(const SieveParams prm) {
       const uint32_t bcnt = S.bcnt;
       const uint64_t bbase = S.bbase;
       if (warp == 0)                                // overlaps the marking
-        claim_item(prm.queue, prm.reqs, prm.P, prm.bcount, total_segs, nreq, s_item[cur ^ 1u], lane);
+        claim_item(prm.queue, prm.reqs, prm.P, prm.bcount, prm.item_lo, item_end, prm.list_seg0, nreq,
+                   s_item[cur ^ 1u], lane);
       const uint32_t nunits = nscan + (bcnt + kBucketUnit - 1) / kBucketUnit;
       const uint32_t o = lane & 7u, h = lane >> 3;
       for (;;) {
@@ -322,14 +325,34 @@ sieve_segments_kernel(const SieveParams prm) {
           const uint32_t r = __ldg(prm.R + 8u * u + o);
           uint32_t s = r >= m ? r - m : r + p - m;
           if (30ull * k0 < (uint64_t)p * p) s = lift_to_square(s, k0, p, o, nbytes);
+          // This lane's stream: bytes j0 + 4 p i = words w0 + p i with one
+          // mask, n of them in the segment.  All 32 streams step p words, so
+          // their banks shift alike: a lane that starts at the step rot
+          // where its stream is in bank `lane` (w0 + p rot = lane mod 32)
+          // stays on a bank of its own while every lane walks on, and each
+          // atomic of the warp takes one shared-memory wavefront instead of
+          // one per lane sharing a bank.  A lane walks steps rot .. n-1,
+          // then wraps to 0 .. rot-1 (wrapped lanes may meet one other lane
+          // on a bank).  With fewer than 32 steps the rotation is taken mod n.
           const uint32_t j0 = s + h * p;
-          if (j0 < nbytes) {
-            const uint32_t c = j0 & 3u;
-            const uint32_t mask = ~(1u << ((c << 3) | o));
-            const uint32_t lim = (nbytes - c + 3u) >> 2;
-            uint32_t w = j0 >> 2;
-#pragma unroll 32
-            for (; w < lim; w += p) atomicAnd(seg + w, mask);
+          const uint32_t c = j0 & 3u;
+          const uint32_t mask = ~(1u << ((c << 3) | o));
+          const uint32_t lim = (nbytes - c + 3u) >> 2;      // word w holds byte 4w + c < nbytes
+          const uint32_t w0 = j0 >> 2;
+          const uint32_t n = w0 < lim ? (lim - w0 + p - 1u) / p : 0u;
+          const uint32_t pinv = p * (2u - p * p);           // p^-1 mod 64 (p odd, p*p = 1 mod 8)
+          uint32_t rot = ((lane - w0) * pinv) & 31u;
+          if (rot >= n) rot = n ? rot % n : 0u;
+          const uint32_t first = n - rot;                    // steps before the wrap
+          const uint32_t k1 = __reduce_min_sync(0xFFFFFFFFu, first);
+          const uint32_t kmax = __reduce_max_sync(0xFFFFFFFFu, n);
+          uint32_t* q = seg + w0 + p * rot;
+          uint32_t k = 0;
+#pragma unroll 8
+          for (; k < k1; ++k, q += p) atomicAnd(q, mask);
+          for (; k < kmax; ++k, q += p) {
+            if (k == first) q -= n * p;                      // wrap to step 0
+            if (k < n) atomicAnd(q, mask);
           }
         } else if (u >= nscan) {
           // bucket list of this segment: primes >= the bucket split whose
@@ -718,20 +741,22 @@ __global__ void __launch_bounds__(kFillPrimes)
 bucket_fill_kernel(const FillParams fp) {
   __shared__ uint32_t cnt[kMaxBucketSegs];
   const uint32_t tid = threadIdx.x;
-  const uint32_t nitems = fp.hdr->nfill;
+  const uint32_t nitems = fp.nitems ? fp.nitems : fp.hdr->nfill;
   for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
     const FillItem item = fp.items[it];
     const ReqDesc R = fp.reqs[item.req];
+    // segments g0..g1 of the window that starts at segment seg0 of the
+    // request; byte offsets below are relative to the window's start k0
     const uint32_t g0 = item.segs & 0xFFFFu, g1 = item.segs >> 16;
     const uint32_t nseg = g1 - g0;
     const uint32_t S = R.seg_bytes;
-    const uint64_t k0 = R.k_lo;
-    const uint32_t total = (uint32_t)(R.k_hi - R.k_lo);
+    const uint64_t k0 = R.k_lo + (uint64_t)fp.seg0 * S;
+    const uint32_t total = (uint32_t)min(R.k_hi - k0, (uint64_t)kMaxBucketSegs * S);
     const uint32_t lo = g0 * S;
     const uint32_t hi = min(total, g1 * S);
     const uint32_t cap = R.bucket_cap;
     uint32_t* const list = fp.bucket + R.bucket_base + (uint64_t)g0 * cap;
-    unsigned int* const gcount = fp.bcount + R.seg_base + g0;
+    unsigned int* const gcount = fp.bcount + R.seg_base + fp.seg0 + g0;
     const float inv_s = 1.0f / (float)S;
     // q = x / S, r = x % S for x < 2^30: a float estimate, corrected once
     auto divmod_s = [&](uint32_t x, uint32_t& r) {

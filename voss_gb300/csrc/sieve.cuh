@@ -158,9 +158,13 @@ struct ReqDesc {
 };
 
 constexpr uint32_t kReqGaps = 1u;
-constexpr uint32_t kMaxBucketSegs = 4096;    // segments of a bucket request (fill-kernel shared counts, 16-bit packing)
-constexpr uint32_t kBucketUnit = 1024;       // list entries per work unit of the sieve kernel
+// Segments whose bucket lists are filled and held at once: a request of
+// more segments is sieved in windows of this many, the lists of one window
+// reusing the same memory (fill-kernel shared counts, 16-bit packing, and
+// window offsets below 2^30 bytes).
+constexpr uint32_t kMaxBucketSegs = 4096;
 constexpr uint32_t kHugeHalf = 32;           // primes per half of a huge-tier work unit (one per lane)
+constexpr uint32_t kBucketUnit = 1024;       // list entries per work unit of the sieve kernel
 constexpr uint32_t kFillPrimes = 256;        // bucket primes per fill work item
 constexpr uint32_t kFillHits = 16384;        // list entries per fill work item, about
 
@@ -255,6 +259,11 @@ struct SieveParams {
   uint32_t* bitmap;          // kFlagBitmap: words of request 0, from k_lo
   const uint32_t* bucket;    // bucket list entries
   const uint32_t* bcount;    // entries written per segment (indexed like segs)
+  // Work items of this launch: [item_lo, min(item_hi, total_segs)), item_hi
+  // 0 standing for total_segs; a windowed plan launches once per window.  The bucket list of segment si of
+  // a request sits at slot si - list_seg0 (the window's first segment).
+  uint64_t item_lo, item_hi;
+  uint64_t list_seg0;
 };
 
 struct FillParams {
@@ -267,6 +276,8 @@ struct FillParams {
   uint32_t* bucket;
   uint32_t* bcount;
   unsigned int* overflow;
+  uint32_t nitems;          // fill items of this launch (0: the batch header's nfill)
+  uint32_t seg0;            // the window's first segment: item segments count from it
 };
 
 }  // namespace vg
