@@ -241,32 +241,38 @@ def secondary(torch, stream, flush):
 
 
 def serving(torch, n=100000):
-    """Served (continuous batching) vs plain one-call-per-request, same stream."""
+    """Served (continuous batching) vs plain one-call-per-request, same stream;
+    latency percentiles under Poisson arrivals at 0.3 / 0.5 / 0.7 / 0.9 of the
+    saturated rate."""
     from voss_gb300.serve import Server, run_plain, run_served, same_answer, serving_mix
     reqs = serving_mix(n)
     warm = serving_mix(64, seed=1)
     run_plain(warm)
     plain, plain_s = run_plain(reqs)
+    q = lambda v, f: v[min(len(v) - 1, int(f * (len(v) - 1) + 0.5))]
+    curve = {}
     with Server() as srv:
         run_served(srv, warm)
         srv.reset_metrics()
         res, lat, wall = run_served(srv, reqs)
         m_sat = srv.metrics()
-        rate = 0.7 * n / wall
-        srv.reset_metrics()
-        res2, lat2, wall2 = run_served(srv, reqs, rate=rate, seed=3)
-        m_rate = srv.metrics()
+        ok = all(same_answer(r, x, y) for r, x, y in zip(reqs, res, plain))
+        for load in (0.3, 0.5, 0.7, 0.9):
+            rate = load * n / wall
+            res2, lat2, wall2 = run_served(srv, reqs, rate=rate, seed=3)
+            ok = ok and all(same_answer(r, x, y) for r, x, y in zip(reqs, res2, plain))
+            lr = sorted(lat2)
+            p50, p99 = q(lr, 0.5) / 1e3, q(lr, 0.99) / 1e3
+            curve[str(load)] = {"rate_req_per_s": rate, "req_per_s": n / wall2, "p50_ms": p50, "p99_ms": p99,
+                                "p99_over_p50": p99 / p50}
     # the same server with each request sieved on its own (no shared pieces):
     # what continuous batching alone gives
     with Server(share=False) as srv:
         run_served(srv, warm)
         res3, lat3, wall3 = run_served(srv, reqs)
-    ok = all(same_answer(r, x, y) for r, x, y in zip(reqs, res, plain)) and \
-        all(same_answer(r, x, y) for r, x, y in zip(reqs, res2, plain)) and \
-        all(same_answer(r, x, y) for r, x, y in zip(reqs, res3, plain))
+    ok = ok and all(same_answer(r, x, y) for r, x, y in zip(reqs, res3, plain))
     ints = sum(r.b - r.a for r in reqs)
-    lat_s, lat_r = sorted(lat), sorted(lat2)
-    q = lambda v, f: v[min(len(v) - 1, int(f * (len(v) - 1) + 0.5))]
+    lat_s = sorted(lat)
     return {"requests": n, "integers": ints, "all_results_equal_plain": ok,
             "plain_req_per_s": n / plain_s, "plain_s": plain_s,
             "served_req_per_s": n / wall, "served_s": wall,
@@ -275,8 +281,10 @@ def serving(torch, n=100000):
             "served_p50_ms": q(lat_s, 0.5) / 1e3, "served_p99_ms": q(lat_s, 0.99) / 1e3,
             "batches": m_sat["batches"], "mean_batch": m_sat["mean_batch"],
             "max_inflight_batches": m_sat["max_inflight_batches"],
-            "poisson_rate_req_per_s": rate, "poisson_req_per_s": n / wall2,
-            "poisson_p50_ms": q(lat_r, 0.5) / 1e3, "poisson_p99_ms": q(lat_r, 0.99) / 1e3}
+            "poisson_curve": curve,
+            "poisson_rate_req_per_s": curve["0.7"]["rate_req_per_s"],
+            "poisson_req_per_s": curve["0.7"]["req_per_s"],
+            "poisson_p50_ms": curve["0.7"]["p50_ms"], "poisson_p99_ms": curve["0.7"]["p99_ms"]}
 
 
 def run_ours(args, rank, world, local_rank):

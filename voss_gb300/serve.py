@@ -8,6 +8,8 @@ mixed request stream: start log-uniform in [0, 10^13], width log-uniform in
 from __future__ import annotations
 
 import ctypes
+import gc
+import sys
 import threading
 import time
 from dataclasses import dataclass
@@ -130,7 +132,21 @@ def run_served(server: Server, reqs: Sequence[Request], rate: Optional[float] = 
     tickets = [0] * len(reqs)
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, len(reqs)) if rate else None
+    # The producer must submit on schedule: no garbage collection pauses and
+    # short interpreter switch intervals while it runs (both are restored).
+    gc_was = gc.isenabled()
+    switch = sys.getswitchinterval()
+    gc.disable()
+    sys.setswitchinterval(2e-4)
+    try:
+        return _run_served(server, reqs, tickets, gaps)
+    finally:
+        sys.setswitchinterval(switch)
+        if gc_was:
+            gc.enable()
 
+
+def _run_served(server, reqs, tickets, gaps):
     def producer():
         t0 = time.perf_counter()
         due = 0.0
