@@ -733,7 +733,8 @@ finalize_kernel(const ReqDesc* __restrict__ reqs, const BatchHdr* __restrict__ h
 // prime walking its eight classes.  Pass 1 counts the hits per segment in
 // shared memory; one global atomic per segment reserves room in that
 // segment's list and leaves the reserved base in the shared counter; pass 2
-// walks the hits again and writes each entry at the counter's next slot.  A
+// walks the hits again and writes each entry at the counter's next slot
+// (two classes at a time, so that two atomic-then-store chains overlap).  A
 // hit's segment and offset advance by p = pq*S + pr without a division.  A
 // list that would overflow its capacity raises *overflow and drops the entry
 // (the host then reruns without lists).
@@ -800,26 +801,34 @@ bucket_fill_kernel(const FillParams fp) {
     // shared sectors.  Spreading the lanes over segments removes the atomic
     // conflicts but scatters the stores, and measured slower.)
     for (int pass = 0; pass < 2; ++pass) {
+      // classes o and o + 4 walk together: two independent chains of
+      // shared atomics and stores per thread
 #pragma unroll
-      for (int o = 0; o < 8; ++o) {
-        uint32_t k = first[o];
-        if (k >= hi) continue;
-        uint32_t off;
-        uint32_t sg = divmod_s(k, off) - g0;                // segment, relative to g0
-        if (pass == 0) {
-          for (; k < hi; k += p) {
-            atomicAdd(&cnt[sg], 1u);
-            off += pr; sg += pq;
-            if (off >= S) { off -= S; ++sg; }
+      for (int o = 0; o < 4; ++o) {
+        uint32_t ka = first[o], kb = first[o + 4];
+        uint32_t offa = 0, offb = 0, sga = 0, sgb = 0;
+        if (ka < hi) sga = divmod_s(ka, offa) - g0;
+        if (kb < hi) sgb = divmod_s(kb, offb) - g0;
+        while (ka < hi || kb < hi) {
+          const bool aa = ka < hi, ab = kb < hi;
+          if (pass == 0) {
+            if (aa) atomicAdd(&cnt[sga], 1u);
+            if (ab) atomicAdd(&cnt[sgb], 1u);
+          } else {
+            uint32_t pa = 0, pb = 0;
+            if (aa) pa = atomicAdd(&cnt[sga], 1u);
+            if (ab) pb = atomicAdd(&cnt[sgb], 1u);
+            if (aa) {
+              if (pa < cap) list[(size_t)sga * cap + pa] = bucket_entry(offa, (uint32_t)o);
+              else atomicOr(fp.overflow, 1u);
+            }
+            if (ab) {
+              if (pb < cap) list[(size_t)sgb * cap + pb] = bucket_entry(offb, (uint32_t)o + 4u);
+              else atomicOr(fp.overflow, 1u);
+            }
           }
-        } else {
-          for (; k < hi; k += p) {
-            const uint32_t pos = atomicAdd(&cnt[sg], 1u);
-            if (pos < cap) list[(size_t)sg * cap + pos] = bucket_entry(off, (uint32_t)o);
-            else atomicOr(fp.overflow, 1u);
-            off += pr; sg += pq;
-            if (off >= S) { off -= S; ++sg; }
-          }
+          if (aa) { ka += p; offa += pr; sga += pq; if (offa >= S) { offa -= S; ++sga; } }
+          if (ab) { kb += p; offb += pr; sgb += pq; if (offb >= S) { offb -= S; ++sgb; } }
         }
       }
       __syncthreads();
