@@ -295,7 +295,7 @@ def run_ours(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     import voss_gb300 as vg
-    from voss_gb300.plan import SievePlan, device_info, smem_peak
+    from voss_gb300.plan import SievePlan, device_info, smem_atomic_cost, smem_peak
     from voss_gb300.shard import gather_merge_many, interleaved_chunks
 
     ranges = interleaved_chunks(0, WIDTH, CHUNK, world, rank) if world > 1 else [(0, WIDTH)]
@@ -357,6 +357,8 @@ def run_ours(args, rank, world, local_rank):
     sieve_ms = statistics.mean(k[0] for k in kt)
     fin_ms = statistics.mean(k[1] for k in kt)
     peaks = smem_peak()
+    # SM clocks per warp-wide shared atomic by bank collisions (the marking's cost model)
+    atom_cost = smem_atomic_cost()
     # algorithmic shared-memory bytes: 8 per candidate clear by a prime
     # 17 < p <= sqrt(b) (a 4-byte read and write), 2 per wheel byte (the
     # pattern fill and the reduction scan)
@@ -407,6 +409,7 @@ def run_ours(args, rank, world, local_rank):
                      "nominal_peak": nominal_gbs, "frac_of_nominal": achieved / nominal_gbs,
                      "nominal_source": "SMs x 128 B/clock x maximum SM clock",
                      "atomic_peak": peaks["atomic_gbs"], "frac_of_atomic_peak": achieved / peaks["atomic_gbs"],
+                     "atomic_clocks_per_warp_op": atom_cost,
                      "sieve_kernel_ms": sieve_ms, "finalize_kernel_ms": fin_ms,
                      "algorithmic_bytes_per_launch": alg_bytes, "clears_per_launch": info["clears"],
                      "wheel_bytes_per_launch": info["wheel_bytes"]},

@@ -243,6 +243,12 @@ void voss_gb300_server_free(voss_gb300_server* s);
  * per step each): the denominators of the sieve's roofline. */
 int voss_gb300_smem_peak(double* ldst_gbs, double* atomic_gbs);
 
+/* SM clocks per warp-wide shared-memory atomicAnd on this GPU when the 32
+ * lanes' banks are distinct, shared 2, 4 or 8 ways, and scattered (clocks[0..4]):
+ * the cost model of the sieve's marking (one wavefront per bank conflict).
+ * No counterpart in the reference. */
+int voss_gb300_smem_atomic_cost(double* clocks);
+
 /* Name of the device the library runs on, and its SM count. */
 int voss_gb300_device_info(char* name, uint32_t name_len, uint32_t* sm_count);
 

@@ -116,6 +116,7 @@ _SIGS = {
     "voss_gb300_plan_free": ([vp], None),
     "voss_gb300_plan_kernel_ms": ([vp, P(ctypes.c_float), P(ctypes.c_float)], c_int),
     "voss_gb300_smem_peak": ([P(ctypes.c_double), P(ctypes.c_double)], c_int),
+    "voss_gb300_smem_atomic_cost": ([P(ctypes.c_double)], c_int),
     "voss_primes_goldbach_minp": ([u64, P(u32), P(u64), P(u32), P(u64), P(u64)], c_int),
     "voss_gb300_goldbach_create": ([u64, P(vp)], c_int),
     "voss_gb300_goldbach_launch": ([vp, vp], c_int),

@@ -832,6 +832,16 @@ extern "C" int voss_gb300_smem_peak(double* ldst_gbs, double* atomic_gbs) {
   }, VOSS_ERR_INTERNAL);
 }
 
+extern "C" int voss_gb300_smem_atomic_cost(double* clocks) {
+  if (!clocks) { set_err("null pointer"); return VOSS_ERR_INVALID_ARG; }
+  return guarded([&] {
+    vg::Engine& E = vg::Engine::for_current_device();
+    std::lock_guard<std::mutex> g(E.mu);
+    vg::smem_atomic_cost(E, clocks);
+    return VOSS_OK;
+  }, VOSS_ERR_INTERNAL);
+}
+
 extern "C" int voss_gb300_device_info(char* name, uint32_t name_len, uint32_t* sm_count) {
   return guarded([&] {
     vg::Engine& E = vg::Engine::for_current_device();

@@ -261,6 +261,9 @@ class Engine {
 };
 
 void smem_peaks(Engine& E, double* ldst_gbs, double* atomic_gbs);
+// SM clocks per warp-wide shared atomicAnd with the lanes' banks distinct,
+// 2-way, 4-way and 8-way shared, and scattered.
+void smem_atomic_cost(Engine& E, double clocks[5]);
 
 void to_public(const ReqResult& r, uint64_t a, uint64_t b, voss_range_stats_t* out);
 

@@ -99,6 +99,13 @@ def smem_peak() -> dict:
     return {"ldst_gbs": a.value, "atomic_gbs": b.value}
 
 
+def smem_atomic_cost() -> dict:
+    """SM clocks per warp-wide shared atomicAnd, by how the lanes' banks collide."""
+    c = (ctypes.c_double * 5)()
+    _capi._check(_capi._lib.voss_gb300_smem_atomic_cost(c), {})
+    return dict(zip(("distinct", "2-way", "4-way", "8-way", "scattered"), list(c)))
+
+
 def device_info() -> dict:
     """Name and SM count of the device the library runs on."""
     name = ctypes.create_string_buffer(256)
