@@ -36,7 +36,7 @@ REGIMES = [
     (MAX_B, U64_MAX, [(10**14, 10**14 + 10**9), (10**14 - 10**10, 10**14)]),
 ]
 SEGS = [65536, 98304, 131072, 163840, 196608, 222848]
-SPLITS = [512, 768, 1024, 2048, 3072, 4096, 6144, 12288]
+SPLITS = [512, 768, 1024, 1400, 1700, 2048, 3072, 4096, 6144, 12288]
 BUCKETS = [0, 221184, 442368, 884736, 1769472]   # bucket-list split (0 = none)
 BUCKET_MARGIN = 0.97                              # a split must beat no lists by 3%
 
