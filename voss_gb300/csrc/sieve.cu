@@ -733,11 +733,57 @@ finalize_kernel(const ReqDesc* __restrict__ reqs, const BatchHdr* __restrict__ h
 // prime walking its eight classes.  Pass 1 counts the hits per segment in
 // shared memory; one global atomic per segment reserves room in that
 // segment's list and leaves the reserved base in the shared counter; pass 2
-// walks the hits again and writes each entry at the counter's next slot
-// (two classes at a time, so that two atomic-then-store chains overlap).  A
+// walks the hits again and writes each entry at the counter's next slot.  A
 // hit's segment and offset advance by p = pq*S + pr without a division.  A
 // list that would overflow its capacity raises *overflow and drops the entry
 // (the host then reruns without lists).
+//
+// The walk takes classes o and o + 4 together, two independent chains of
+// atomic-then-store per thread: both step unconditionally while both have
+// hits left (each chain's count of hits is known up front), then the longer
+// one finishes alone.  (Lanes of a warp hold primes of nearly the same size
+// and walk in step, so many of them meet on one segment counter at a time;
+// the counter then hands them consecutive slots and their entries leave in
+// shared sectors.  Spreading the lanes over segments removes the atomic
+// conflicts but scatters the stores, and measured slower.)
+struct FillChain {
+  uint32_t sg, off, n;       // segment (relative to the item's first), offset, hits left
+};
+
+template <bool kWrite>
+__device__ __forceinline__ void fill_step(FillChain& c, uint32_t o, uint32_t* cnt, uint32_t* list,
+                                          uint32_t cap, unsigned int* overflow, uint32_t S,
+                                          uint32_t pq, uint32_t pr) {
+  if (kWrite) {
+    const uint32_t pos = atomicAdd(&cnt[c.sg], 1u);
+    if (pos < cap) list[c.sg * cap + pos] = bucket_entry(c.off, o);
+    else atomicOr(overflow, 1u);
+  } else {
+    atomicAdd(&cnt[c.sg], 1u);
+  }
+  c.off += pr;
+  const uint32_t carry = c.off >= S ? 1u : 0u;
+  c.off -= carry ? S : 0u;
+  c.sg += pq + carry;
+}
+
+template <bool kWrite>
+__device__ __forceinline__ void fill_pass(const FillChain (&start)[8], uint32_t* cnt, uint32_t* list,
+                                          uint32_t cap, unsigned int* overflow, uint32_t S,
+                                          uint32_t pq, uint32_t pr) {
+#pragma unroll
+  for (uint32_t o = 0; o < 4; ++o) {
+    FillChain a = start[o], b = start[o + 4];
+    const uint32_t both = min(a.n, b.n);
+    for (uint32_t t = 0; t < both; ++t) {
+      fill_step<kWrite>(a, o, cnt, list, cap, overflow, S, pq, pr);
+      fill_step<kWrite>(b, o + 4u, cnt, list, cap, overflow, S, pq, pr);
+    }
+    for (uint32_t t = both; t < a.n; ++t) fill_step<kWrite>(a, o, cnt, list, cap, overflow, S, pq, pr);
+    for (uint32_t t = both; t < b.n; ++t) fill_step<kWrite>(b, o + 4u, cnt, list, cap, overflow, S, pq, pr);
+  }
+}
+
 __global__ void __launch_bounds__(kFillPrimes)
 bucket_fill_kernel(const FillParams fp) {
   __shared__ uint32_t cnt[kMaxBucketSegs];
@@ -756,6 +802,8 @@ bucket_fill_kernel(const FillParams fp) {
     const uint32_t lo = g0 * S;
     const uint32_t hi = min(total, g1 * S);
     const uint32_t cap = R.bucket_cap;
+    // the item's lists, segment g at g * cap (the host keeps a window's
+    // entries below 2^32)
     uint32_t* const list = fp.bucket + R.bucket_base + (uint64_t)g0 * cap;
     unsigned int* const gcount = fp.bcount + R.seg_base + fp.seg0 + g0;
     const float inv_s = 1.0f / (float)S;
@@ -779,67 +827,34 @@ bucket_fill_kernel(const FillParams fp) {
       low = 30ull * k0 < (uint64_t)p * p;
       pq = divmod_s(p, pr);
     }
-    // first hit at or after segment g0 of each class, kept for both passes
-    // (hi = none); the eight residue loads issue together
-    uint32_t first[8];
-    if (valid) load_residues(fp.R, i, first);
+    // first hit at or after byte lo of each class and the number of hits
+    // below hi, kept for both passes; the eight residue loads issue together
+    uint32_t r8[8];
+    if (valid) load_residues(fp.R, i, r8);
+    FillChain ch[8];
 #pragma unroll
     for (int o = 0; o < 8; ++o) {
-      uint32_t k = hi;
+      ch[o].sg = 0; ch[o].off = 0; ch[o].n = 0;
       if (valid) {
-        const uint32_t r = first[o];
-        k = r >= m ? r - m : r + p - m;
+        const uint32_t r = r8[o];
+        uint32_t k = r >= m ? r - m : r + p - m;
         if (low) k = lift_to_square(k, k0, p, o, total);
         if (k < lo) k += ((lo - k + p - 1) / p) * p;
-        k = min(k, hi);
-      }
-      first[o] = k;
-    }
-    // (Lanes of a warp hold primes of nearly the same size and walk in
-    // step, so many of them meet on one segment counter at a time; the
-    // counter then hands them consecutive slots and their entries leave in
-    // shared sectors.  Spreading the lanes over segments removes the atomic
-    // conflicts but scatters the stores, and measured slower.)
-    for (int pass = 0; pass < 2; ++pass) {
-      // classes o and o + 4 walk together: two independent chains of
-      // shared atomics and stores per thread
-#pragma unroll
-      for (int o = 0; o < 4; ++o) {
-        uint32_t ka = first[o], kb = first[o + 4];
-        uint32_t offa = 0, offb = 0, sga = 0, sgb = 0;
-        if (ka < hi) sga = divmod_s(ka, offa) - g0;
-        if (kb < hi) sgb = divmod_s(kb, offb) - g0;
-        while (ka < hi || kb < hi) {
-          const bool aa = ka < hi, ab = kb < hi;
-          if (pass == 0) {
-            if (aa) atomicAdd(&cnt[sga], 1u);
-            if (ab) atomicAdd(&cnt[sgb], 1u);
-          } else {
-            uint32_t pa = 0, pb = 0;
-            if (aa) pa = atomicAdd(&cnt[sga], 1u);
-            if (ab) pb = atomicAdd(&cnt[sgb], 1u);
-            if (aa) {
-              if (pa < cap) list[(size_t)sga * cap + pa] = bucket_entry(offa, (uint32_t)o);
-              else atomicOr(fp.overflow, 1u);
-            }
-            if (ab) {
-              if (pb < cap) list[(size_t)sgb * cap + pb] = bucket_entry(offb, (uint32_t)o + 4u);
-              else atomicOr(fp.overflow, 1u);
-            }
-          }
-          if (aa) { ka += p; offa += pr; sga += pq; if (offa >= S) { offa -= S; ++sga; } }
-          if (ab) { kb += p; offb += pr; sgb += pq; if (offb >= S) { offb -= S; ++sgb; } }
+        if (k < hi) {
+          ch[o].n = (hi - 1u - k) / p + 1u;
+          ch[o].sg = divmod_s(k, ch[o].off) - g0;
         }
       }
-      __syncthreads();
-      if (pass == 0) {
-        for (uint32_t g = tid; g < nseg; g += blockDim.x) {
-          const uint32_t c = cnt[g];
-          cnt[g] = c ? atomicAdd(gcount + g, c) : 0u;
-        }
-        __syncthreads();
-      }
     }
+    fill_pass<false>(ch, cnt, list, cap, fp.overflow, S, pq, pr);
+    __syncthreads();
+    for (uint32_t g = tid; g < nseg; g += blockDim.x) {
+      const uint32_t c = cnt[g];
+      cnt[g] = c ? atomicAdd(gcount + g, c) : 0u;
+    }
+    __syncthreads();
+    fill_pass<true>(ch, cnt, list, cap, fp.overflow, S, pq, pr);
+    __syncthreads();
   }
 }
 
