@@ -255,8 +255,11 @@ BucketPlan Engine::bucket_plan(const Config& c, uint64_t b, uint32_t nprimes, ui
   // the capacity leaves a margin of many standard deviations
   const double mean = 8.0 * seg_bytes * (hInvPrefix[nprimes] - hInvPrefix[idx]);
   const double cap = (mean * 1.25 + 32.0 * std::sqrt(mean) + 1024.0) * cfg.bucket_cap_pct / 100.0;
+  const uint32_t c32 = std::max<uint32_t>(32u, ((uint32_t)cap + 31u) & ~31u);
+  // the fill kernel indexes a window's lists with 32-bit offsets
+  if ((uint64_t)c32 * std::min<uint64_t>(nseg, kMaxBucketSegs) >= (1ull << 32)) return bp;
   bp.bucket_idx = idx;
-  bp.cap = std::max<uint32_t>(32u, ((uint32_t)cap + 31u) & ~31u);
+  bp.cap = c32;
   return bp;
 }
 
