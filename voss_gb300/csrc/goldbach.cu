@@ -77,6 +77,9 @@ constexpr int kGbWords = 8;                                  // U words per thre
 constexpr uint32_t kGbTile = kGbThreads * kGbWords * 32;     // even n per tile
 constexpr uint32_t kGbSmemHist = 4096;                       // p < 4096 counted in smem
 constexpr size_t kGbSmemBytes = kGbSmemHist * 4;
+// The dense bit-set walk stops once at most this many n of a tile are open;
+// the rest are tested a warp per n.
+constexpr uint32_t kGbList = 256;
 // Zero words before and after the odd-number bitmap: a thread's window words
 // (floor(base/32) + kGbWords*tid .. + kGbWords) then never leave the buffer,
 // with no bounds test (base >= -kGbTile/2 in the first tile, so at most
@@ -110,11 +113,15 @@ goldbach_minp_kernel(const uint32_t* __restrict__ odd,
                      uint64_t ntiles, GbOut out) {
   extern __shared__ __align__(16) uint32_t gb_smem[];
   uint32_t* shist = gb_smem;                                          // kGbSmemHist
+  __shared__ uint32_t s_list[kGbList];         // open n of the sparse phase (tile offsets)
+  __shared__ uint32_t s_open[3], s_cnt;
   const uint32_t tid = threadIdx.x, lane = tid & 31u;
   const uint64_t n_last = N & ~1ull;           // largest even n
   uint32_t lmax = 0;
+  uint32_t chk = 0;                            // checks so far (the same in every thread)
   unsigned long long lsum = 0, lprobes = 0;
   for (uint32_t i = tid; i < kGbSmemHist; i += kGbThreads) shist[i] = 0;
+  if (tid < 3) s_open[tid] = 0;
   __syncthreads();
 
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -129,11 +136,28 @@ goldbach_minp_kernel(const uint32_t* __restrict__ odd,
       U[q] = t0 >= tcount ? 0u : (tcount - t0 >= 32 ? 0xFFFFFFFFu : ((1u << (tcount - t0)) - 1u));
     }
     bool exhausted = true;
-    for (uint32_t pi = 0; pi < noddp; ++pi) {
+    bool sparse = false;
+    uint32_t pi = 0;
+    if (tid == 0) s_cnt = 0;                   // list of the sparse phase (ordered by the first check's barrier)
+    for (; pi < noddp; ++pi) {
       const uint32_t p = __ldg(oddp + pi);
       if (2ull * p > nmax) { exhausted = false; break; }
       if ((pi & 7u) == 0) {
-        if (!__syncthreads_or(any_open(U))) { exhausted = false; break; }
+        // the tile's open n, summed over the block into one of three
+        // counters taken in turn over all checks of all tiles (the next one
+        // is cleared here: every thread read it two checks ago, and nobody
+        // adds to it before this check's barrier)
+        const uint32_t r = chk++ % 3u;
+        uint32_t mine = 0;
+#pragma unroll
+        for (int q = 0; q < kGbWords; ++q) mine += __popc(U[q]);
+        mine = __reduce_add_sync(0xFFFFFFFFu, mine);
+        if (lane == 0 && mine) atomicAdd(&s_open[r], mine);
+        if (tid == 0) s_open[(r + 1u) % 3u] = 0;
+        __syncthreads();
+        const uint32_t open = s_open[r];
+        if (open == 0) { exhausted = false; break; }
+        if (open <= kGbList) { sparse = true; break; }
       }
       // bit j of this thread's word q is n = n0 + 2*(32*(4*tid + q) + j); its
       // partner n - p is odd bit base + 32*(4*tid + q) + j, so the thread's
@@ -171,6 +195,82 @@ goldbach_minp_kernel(const uint32_t* __restrict__ odd,
         if (p < kGbSmemHist) atomicAdd(&shist[p], wres);
         else atomicAdd(&out.hist[p], (unsigned long long)wres);
       }
+    }
+    if (sparse) {
+      // Few n are left open: gather them into a shared list, then eight
+      // lanes per n test eight primes at a time (from the first prime not
+      // yet tried) and take the smallest hit by a ballot.  Same bound as
+      // above (2p <= the tile's largest n), same outputs.
+#pragma unroll
+      for (int q = 0; q < kGbWords; ++q) {
+        uint32_t u = U[q];
+        U[q] = 0;
+        while (u) {
+          const uint32_t j = (uint32_t)__ffs(u) - 1u;
+          u &= u - 1u;
+          s_list[atomicAdd(&s_cnt, 1u)] = 32u * (tid * kGbWords + q) + j;
+        }
+      }
+      __syncthreads();
+      const uint32_t cnt = s_cnt;
+      // four n per warp at a time, eight lanes (eight primes per step) each,
+      // so that four chains of loads are in flight
+      const uint32_t warp = tid >> 5, sub = lane >> 3, sl = lane & 7u;
+      const uint32_t smask = 0xFFu << (8u * sub);
+      constexpr uint32_t kSlots = 4u * (kGbThreads / 32);
+      uint32_t e = 4u * warp + sub;
+      bool active = e < cnt;
+      uint32_t t = active ? s_list[e] : 0u;
+      uint32_t pj = pi;
+      while (__any_sync(0xFFFFFFFFu, active)) {
+        const uint64_t n = n0 + 2ull * t;
+        const uint32_t pk = pj + sl;
+        const bool listed = active && pk < noddp;
+        const uint32_t p = listed ? __ldg(oddp + pk) : 0xFFFFFFFFu;
+        const bool in = listed && 2ull * p <= nmax;
+        bool ok = false;
+        if (in && p < n) {                                         // n - p <= 0 is no prime
+          const uint64_t bi = (n - p - 1) / 2;                    // odd bit of n - p, < N / 2
+          ok = (__ldg(odd + (bi >> 5)) >> (uint32_t)(bi & 31u)) & 1u;
+        }
+        const uint32_t hit = __ballot_sync(0xFFFFFFFFu, ok) & smask;
+        const uint32_t oob = __ballot_sync(0xFFFFFFFFu, listed && !in) & smask;
+        const uint32_t ool = __ballot_sync(0xFFFFFFFFu, active && pk >= noddp) & smask;
+        const uint32_t pm = __shfl_sync(0xFFFFFFFFu, p, hit ? __ffs(hit) - 1u : lane);
+        if (active) {
+          bool done = true;
+          if (hit) {
+            if (sl == 0) {
+              if (out.minp) out.minp[obase + t] = pm;
+              lmax = max(lmax, pm);
+              lsum += pm;
+              if (pm < kGbSmemHist) atomicAdd(&shist[pm], 1u);
+              else atomicAdd(&out.hist[pm], 1ull);
+            }
+          } else if (oob | ool) {
+            if (sl == 0) {
+              // primes past the bound first: a counterexample; the list ended first: an error
+              if (oob && (!ool || __ffs(oob) < __ffs(ool))) {
+                const unsigned long long slot = atomicAdd(out.n_ce, 1ull);
+                if (slot < out.ce_cap) out.ce[slot] = n;
+              } else {
+                atomicOr(out.err, 1u);
+              }
+            }
+          } else {
+            done = false;
+            pj += 8u;
+          }
+          if (sl == 0) ++lprobes;
+          if (done) {
+            e += kSlots;
+            active = e < cnt;
+            t = active ? s_list[e] : 0u;
+            pj = pi;
+          }
+        }
+      }
+      __syncthreads();                           // the list is reused by the next tile
     }
     // Whatever is left: counterexamples, unless the prime list ran out first.
 #pragma unroll
