@@ -738,10 +738,10 @@ finalize_kernel(const ReqDesc* __restrict__ reqs, const BatchHdr* __restrict__ h
 // list that would overflow its capacity raises *overflow and drops the entry
 // (the host then reruns without lists).
 //
-// The walk takes four classes together (o, o + 2, o + 4, o + 6), four
-// independent chains of atomic-then-store per thread: all step
-// unconditionally while all have hits left (each chain's count of hits is
-// known up front), then each finishes alone under its own predicate.  (Lanes of a warp hold primes of nearly the same size
+// The walk takes the eight classes together, eight independent chains of
+// atomic-then-store per thread: all step unconditionally while all have hits
+// left (each chain's count of hits is known up front), then each finishes
+// under its own predicate.  (Lanes of a warp hold primes of nearly the same size
 // and walk in step, so many of them meet on one segment counter at a time;
 // the counter then hands them consecutive slots and their entries leave in
 // shared sectors.  Spreading the lanes over segments removes the atomic
@@ -771,23 +771,18 @@ template <bool kWrite>
 __device__ __forceinline__ void fill_pass(const FillChain (&start)[8], uint32_t* cnt, uint32_t* list,
                                           uint32_t cap, unsigned int* overflow, uint32_t S,
                                           uint32_t pq, uint32_t pr) {
+  FillChain c[8];
+  uint32_t all = start[0].n, most = start[0].n;
 #pragma unroll
-  for (uint32_t o = 0; o < 2; ++o) {
-    FillChain c0 = start[o], c1 = start[o + 2], c2 = start[o + 4], c3 = start[o + 6];
-    const uint32_t all = min(min(c0.n, c1.n), min(c2.n, c3.n));
-    const uint32_t most = max(max(c0.n, c1.n), max(c2.n, c3.n));
-    for (uint32_t t = 0; t < all; ++t) {
-      fill_step<kWrite>(c0, o, cnt, list, cap, overflow, S, pq, pr);
-      fill_step<kWrite>(c1, o + 2u, cnt, list, cap, overflow, S, pq, pr);
-      fill_step<kWrite>(c2, o + 4u, cnt, list, cap, overflow, S, pq, pr);
-      fill_step<kWrite>(c3, o + 6u, cnt, list, cap, overflow, S, pq, pr);
-    }
-    for (uint32_t t = all; t < most; ++t) {
-      if (t < c0.n) fill_step<kWrite>(c0, o, cnt, list, cap, overflow, S, pq, pr);
-      if (t < c1.n) fill_step<kWrite>(c1, o + 2u, cnt, list, cap, overflow, S, pq, pr);
-      if (t < c2.n) fill_step<kWrite>(c2, o + 4u, cnt, list, cap, overflow, S, pq, pr);
-      if (t < c3.n) fill_step<kWrite>(c3, o + 6u, cnt, list, cap, overflow, S, pq, pr);
-    }
+  for (int o = 0; o < 8; ++o) { c[o] = start[o]; all = min(all, c[o].n); most = max(most, c[o].n); }
+  for (uint32_t t = 0; t < all; ++t) {
+#pragma unroll
+    for (uint32_t o = 0; o < 8; ++o) fill_step<kWrite>(c[o], o, cnt, list, cap, overflow, S, pq, pr);
+  }
+  for (uint32_t t = all; t < most; ++t) {
+#pragma unroll
+    for (uint32_t o = 0; o < 8; ++o)
+      if (t < c[o].n) fill_step<kWrite>(c[o], o, cnt, list, cap, overflow, S, pq, pr);
   }
 }
 
