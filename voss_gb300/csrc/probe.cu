@@ -94,7 +94,11 @@ smem_atomic_cost_kernel(uint32_t iters, uint32_t pattern, unsigned long long* cy
   if (pattern == 1) bank = lane & 15u;                    // 2-way
   else if (pattern == 2) bank = lane & 7u;                // 4-way
   else if (pattern == 3) bank = lane & 3u;                // 8-way
-  else if (pattern == 4) bank = (lane * 2654435761u + warp * 40503u) >> 27;   // scattered (hash)
+  else if (pattern == 4) {                               // scattered: a hash of (warp, lane)
+    uint32_t h = (lane + 1u) * 0x9E3779B9u ^ (warp + 1u) * 0x85EBCA6Bu;
+    h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
+    bank = h >> 27;
+  }
   uint32_t* p = s + row * 32u + bank;
   const uint32_t mask = ~(1u << lane);
   const unsigned long long t0 = clock64();
