@@ -97,13 +97,28 @@ def test_poisson_arrivals_and_admission_limits(vg):
 
 
 @pytest.mark.gpu
-def test_server_rejects_oversized_and_bad_ops(vg):
-    from voss_gb300.serve import Server
-    with Server(slots=1, max_segments=64) as srv:
-        with pytest.raises(vg.VossError):
-            srv.submit(0, 10**11)                  # needs more than 64 segments
+def test_server_splits_wide_requests_and_rejects_bad_ones(vg):
+    """A request wider than half a batch runs as consecutive pieces in several
+    batches, interleaved with other requests; its answer is the one it gets
+    alone.  Unknown ops, ends beyond the limit and collected tickets fail."""
+    from voss_gb300.serve import OP_CHEBYSHEV, OP_COUNT, OP_GAP_HIST, OP_TWINS, Request, Server, same_answer
+    reqs = [Request(0, 10**11, OP_TWINS), Request(999, 12345, OP_COUNT),
+            Request(5 * 10**11 + 7, 5 * 10**11 + 3 * 10**10, OP_GAP_HIST),
+            Request(10**6, 10**6 + 10**5, OP_GAP_HIST), Request(10**12, 10**12 + 2 * 10**10 + 1, OP_CHEBYSHEV),
+            Request(10**14 - 10**9, 10**14 + 10**9, OP_TWINS)]
+    with Server(slots=2, max_segments=64) as srv:
+        tickets = [srv.submit(r.a, r.b, r.op) for r in reqs]
+        for r, t in zip(reqs, tickets):
+            got, lat = srv.result(t)
+            assert lat > 0
+            assert same_answer(r, got, vg.range_stats(r.a, r.b)), r
+        m = srv.metrics()
+        # about 700 pieces of at most 32 segments, two to a batch of 64 segments
+        assert m["completed"] == len(reqs) and m["batches"] > 300
         with pytest.raises(vg.VossError):
             srv.submit(0, 1000, 9)
+        with pytest.raises(vg.VossError):
+            srv.submit(0, 10**15)
         t = srv.submit(0, 1000, 0)
         got, lat = srv.result(t)
         assert got.count == 168

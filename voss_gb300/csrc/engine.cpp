@@ -794,6 +794,33 @@ const ReqResult* Engine::run(uint32_t n, const uint64_t* a, const uint64_t* b,
   return r;
 }
 
+ReqResult merge_ordered(const ReqResult* parts, size_t n, bool gaps) {
+  ReqResult m;
+  std::memset(&m, 0, sizeof(m));
+  uint64_t bg = 0, bs = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const ReqResult& r = parts[i];
+    m.count += r.count;
+    m.c41 += r.c41; m.c43 += r.c43; m.c31 += r.c31; m.c32 += r.c32;
+    if (!r.count) continue;
+    if (gaps) {
+      for (int b = 0; b < kHistBins; ++b) m.hist[b] += r.hist[b];
+      if (m.last) {                               // the gap into this piece (its start is the earlier)
+        const uint64_t g = r.first - m.last;
+        m.hist[std::min<uint64_t>(g >> 1, kHistBins - 1)]++;
+        if (g > bg) { bg = g; bs = m.last; }
+      }
+      if (r.max_gap > bg) { bg = r.max_gap; bs = r.max_gap_start; }
+    }
+    if (!m.first) m.first = r.first;
+    m.last = r.last;
+  }
+  m.max_gap = bg;
+  m.max_gap_start = bg ? bs : 0;
+  m.num_gaps = m.count ? m.count - 1 : 0;
+  return m;
+}
+
 void to_public(const ReqResult& r, uint64_t a, uint64_t b, voss_range_stats_t* o) {
   std::memset(o, 0, sizeof(*o));
   o->a = a;

@@ -266,6 +266,11 @@ void smem_peaks(Engine& E, double* ldst_gbs, double* atomic_gbs);
 void smem_atomic_cost(Engine& E, double clocks[5]);
 
 void to_public(const ReqResult& r, uint64_t a, uint64_t b, voss_range_stats_t* out);
+// The result of a range from the results of its consecutive pieces (in order):
+// counts add; with gaps, each junction between pieces that hold primes adds
+// one gap, and the largest gap is the largest of the pieces' and the
+// junctions' (the earliest on ties), as within one range.
+ReqResult merge_ordered(const ReqResult* parts, size_t n, bool gaps);
 
 // Launchers defined in sieve.cu.
 size_t sieve_smem_bytes(uint32_t seg_bytes, uint32_t threads);

@@ -88,28 +88,64 @@ Server::~Server() {
 uint64_t Server::submit(uint64_t a, uint64_t b, uint32_t op) {
   if (b > kMaxB) throw Error(VOSS_ERR_OUT_OF_RANGE, "range end exceeds 10^14 + 10^10 + 1");
   if (op > kOpChebyshev) throw Error(VOSS_ERR_INVALID_ARG, "unknown request op");
-  const uint64_t segs = slots[0]->plan.segments_for(a, b);
-  if (segs > cfg.max_segs)
-    throw Error(VOSS_ERR_OUT_OF_RANGE, "range needs more segments than a server batch holds");
-  Ticket t;
-  t.a = a;
-  t.b = b;
-  t.op = op;
-  t.segs = segs;
-  // bucket lists that do not fit a slot's arena are not used (the plan skips them)
-  uint64_t bb = slots[0]->plan.list_bytes_for(a, b);
-  if (bb > cfg.bucket_bytes) bb = 0;
-  t.bytes = request_bytes(segs) + bb;
-  t.t_submit = now_us();
+  const Plan& plan = slots[0]->plan;
+  // A request wider than half a batch runs as consecutive pieces of at most
+  // half a batch each (batches sieve with the largest segment S, and a piece
+  // of (half S - 2) wheel bytes spans at most half segments), so that other
+  // requests' batches interleave with them.
+  const uint64_t half = std::max<uint64_t>(cfg.max_segs / 2, 1);
+  std::vector<std::pair<uint64_t, uint64_t>> pieces;
+  if (b > a && plan.segments_for(a, b) > half) {
+    const uint64_t S = E.cfg.seg_bytes;
+    const uint64_t w = 30ull * std::max<uint64_t>(half * S, 3) - 60ull;   // integers per piece
+    for (uint64_t x = a; x < b; x += std::min(w, b - x)) pieces.emplace_back(x, std::min(b, x + w));
+  } else {
+    pieces.emplace_back(a, b);
+  }
+  std::vector<Ticket> parts(pieces.size());
+  for (size_t i = 0; i < pieces.size(); ++i) {
+    Ticket& t = parts[i];
+    t.a = pieces[i].first;
+    t.b = pieces[i].second;
+    t.op = op;
+    t.segs = plan.segments_for(t.a, t.b);
+    if (t.segs > cfg.max_segs)
+      throw Error(VOSS_ERR_INTERNAL, "a request piece needs more segments than a server batch holds");
+    // bucket lists that do not fit a slot's arena are not used (the plan skips them)
+    uint64_t bb = plan.list_bytes_for(t.a, t.b);
+    if (bb > cfg.bucket_bytes) bb = 0;
+    t.bytes = request_bytes(t.segs) + bb;
+  }
+  const double now = now_us();
   uint64_t id;
   {
     std::lock_guard<std::mutex> g(mu);
     if (stop) throw Error(VOSS_ERR_INVALID_ARG, "server is shutting down");
     id = next_id++;
-    tickets.emplace(id, t);
-    pending.push_back(id);
+    if (parts.size() == 1) {
+      parts[0].t_submit = now;
+      tickets.emplace(id, parts[0]);
+      pending.push_back(id);
+    } else {
+      Ticket t;
+      t.a = a;
+      t.b = b;
+      t.op = op;
+      t.t_submit = now;
+      t.npieces = (uint32_t)parts.size();
+      t.parts.resize(parts.size());
+      tickets.emplace(id, std::move(t));
+      for (size_t i = 0; i < parts.size(); ++i) {
+        const uint64_t cid = next_id++;
+        parts[i].parent = id;
+        parts[i].index = (uint32_t)i;
+        parts[i].t_submit = now;
+        tickets.emplace(cid, parts[i]);
+        pending.push_back(cid);
+      }
+    }
     ++submitted;
-    if (!first_submit) first_submit = t.t_submit;
+    if (!first_submit) first_submit = now;
   }
   cv_work.notify_one();
   return id;
@@ -169,10 +205,45 @@ void Server::reset_metrics() {
   std::lock_guard<std::mutex> g(mu);
   lat.clear();
   completed = batches = batched_requests = 0;
-  submitted = pending.size() + inflight_requests;
+  submitted = 0;                          // requests not yet done (a split one counts once)
+  for (const auto& kv : tickets)
+    if (!kv.second.parent && !kv.second.done) ++submitted;
   first_submit = last_done = 0;
   max_inflight = 0;
   peak_bytes = 0;
+}
+
+// Called with mu held: a batch entry is done (r = its result, or null with
+// err).  A piece hands its result to its request, which completes with its
+// last piece; the piece's own ticket goes.
+void Server::finish_ticket(uint64_t id, Ticket& tk, const ReqResult* r, const std::string& err, double t) {
+  if (!tk.parent) {
+    if (r) to_public(*r, tk.a, tk.b, &tk.res);
+    else { tk.error = true; tk.message = err; }
+    tk.done = true;
+    tk.t_done = t;
+    lat.push_back(t - tk.t_submit);
+    ++completed;
+    return;
+  }
+  const uint64_t pid = tk.parent;
+  const uint32_t idx = tk.index;
+  Ticket& par = tickets.at(pid);
+  if (r) par.parts[idx] = *r;
+  else if (!par.error) { par.error = true; par.message = err; }
+  ++par.pieces_done;
+  tickets.erase(id);                     // tk is gone from here on
+  if (par.pieces_done < par.npieces) return;
+  if (!par.error) {
+    const bool gaps = par.op == kOpTwins || par.op == kOpGapHist;
+    const ReqResult m = merge_ordered(par.parts.data(), par.parts.size(), gaps);
+    to_public(m, par.a, par.b, &par.res);
+  }
+  std::vector<ReqResult>().swap(par.parts);
+  par.done = true;
+  par.t_done = t;
+  lat.push_back(t - par.t_submit);
+  ++completed;
 }
 
 void Server::retire(Slot& s) {
@@ -200,15 +271,8 @@ void Server::retire(Slot& s) {
   }
   const double t = now_us();
   std::lock_guard<std::mutex> g(mu);
-  for (size_t i = 0; i < s.ids.size(); ++i) {
-    Ticket& tk = tickets.at(s.ids[i]);
-    if (r) to_public(r[i], tk.a, tk.b, &tk.res);
-    else { tk.error = true; tk.message = err; }
-    tk.done = true;
-    tk.t_done = t;
-    lat.push_back(t - tk.t_submit);
-  }
-  completed += s.ids.size();
+  for (size_t i = 0; i < s.ids.size(); ++i)
+    finish_ticket(s.ids[i], tickets.at(s.ids[i]), r ? r + i : nullptr, err, t);
   inflight_requests -= s.ids.size();
   last_done = t;
   inflight_bytes -= s.bytes;
@@ -264,13 +328,7 @@ bool Server::admit(Slot& s) {
   } catch (const std::exception& e) {
     std::lock_guard<std::mutex> g(mu);
     const double t = now_us();
-    for (uint64_t id : s.ids) {
-      Ticket& tk = tickets.at(id);
-      tk.error = true;
-      tk.message = e.what();
-      tk.done = true;
-      tk.t_done = t;
-    }
+    for (uint64_t id : s.ids) finish_ticket(id, tickets.at(id), nullptr, e.what(), t);
     inflight_requests -= s.ids.size();
     inflight_bytes -= bytes;
     --inflight;

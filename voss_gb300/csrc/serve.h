@@ -50,6 +50,13 @@ class Server {
     bool done = false, error = false;
     std::string message;
     voss_range_stats_t res{};
+    // A request wider than half a batch runs as consecutive pieces, each an
+    // internal ticket (parent = the request's id, index = its place); the
+    // request collects their results and is done with the last one.
+    uint64_t parent = 0;
+    uint32_t index = 0;
+    uint32_t npieces = 0, pieces_done = 0;
+    std::vector<ReqResult> parts;
   };
   struct Slot {
     Plan plan;
@@ -64,6 +71,7 @@ class Server {
   void loop();
   void retire(Slot& s);
   bool admit(Slot& s);
+  void finish_ticket(uint64_t id, Ticket& tk, const ReqResult* r, const std::string& err, double t);
 
   Engine& E;
   ServerConfig cfg;
