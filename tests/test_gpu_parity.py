@@ -235,6 +235,27 @@ def test_context_1e12_reference_values(vg):
         assert all(g.gap >= 500 for g in gaps)
 
 
+def test_context_1e12_in_windows(vg):
+    """The same reference values with bucket lists forced on and 64 KiB
+    segments: Context(10^12) then runs in about 125 windows of 4096
+    segments, each filling and reusing one list arena."""
+    base = _with_config(vg, seg_bytes=65536, tier_split=1024, bucket_split=131072, auto_tune=0)
+    try:
+        from voss_gb300.plan import SievePlan
+        plan = SievePlan([(1, 10**12 + 1)])
+        info = plan.info()
+        plan.close()
+        assert info["segments"] > 100 * 4096 and info["kernels_per_run"] > 200, info
+        with vg.Context(10**12) as ctx:
+            assert ctx.prime_count() == 37607912018
+            assert ctx.twins() == 1870585220
+            gaps = ctx.large_gaps()
+            assert len(gaps) == 11
+            assert (gaps[0].gap, gaps[0].position) == (540, 738832928467)
+    finally:
+        vg.primes.set_config(**base)
+
+
 @pytest.mark.slow
 def test_prime_count_1e13(vg):
     # pi(10^13) = 346 065 536 839, the reference's recorded value (STATE.md:103)
