@@ -204,8 +204,8 @@ void voss_gb300_goldbach_free(voss_gb300_goldbach* g);
 
 typedef struct {
     uint32_t slots;               /* batches in flight (default 4) */
-    uint32_t max_batch;           /* requests per batch (default 256) */
-    uint64_t max_segments;        /* segments per batch (default 32768) */
+    uint32_t max_batch;           /* requests per batch (default 1024) */
+    uint64_t max_segments;        /* segments per batch (default 65536) */
     uint64_t memory_budget;       /* device bytes over all batches in flight */
     uint32_t use_graphs;          /* replay a captured CUDA graph per batch */
     uint64_t bucket_bytes;        /* bucket-list arena per slot (default 256 MiB) */

@@ -21,8 +21,8 @@ constexpr uint32_t kOpChebyshev = VOSS_OP_CHEBYSHEV;
 
 struct ServerConfig {
   uint32_t slots = 4;            // batches in flight at once
-  uint32_t max_batch = 256;      // requests per batch
-  uint64_t max_segs = 1u << 15;  // segments per batch
+  uint32_t max_batch = 1024;     // requests per batch
+  uint64_t max_segs = 1u << 16;  // segments per batch
   uint64_t mem_budget = 1ull << 30;   // device bytes over all batches in flight
   uint32_t use_graphs = 1;
   uint64_t bucket_bytes = 256ull << 20;   // bucket-list arena per slot

@@ -56,7 +56,7 @@ for _n in ("voss_gb300_server_create", "voss_gb300_server_submit", "voss_gb300_s
 
 
 class Server:
-    def __init__(self, slots: int = 4, max_batch: int = 256, max_segments: int = 1 << 15,
+    def __init__(self, slots: int = 4, max_batch: int = 1024, max_segments: int = 1 << 16,
                  memory_budget: int = 1 << 30, use_graphs: bool = True, bucket_bytes: int = 256 << 20,
                  share: bool = True):
         cfg = ServerConfig(slots, max_batch, max_segments, memory_budget, 1 if use_graphs else 0,
