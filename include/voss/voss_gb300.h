@@ -196,7 +196,10 @@ void voss_gb300_goldbach_free(voss_gb300_goldbach* g);
  * records, accumulators, results and bucket lists.  The reference has no counterpart: it
  * serves one Context at a time (context.cu:212-559).  Every request gets the
  * full voss_range_stats_t; for COUNT and CHEBYSHEV requests the gap fields
- * are not computed (zero). */
+ * are not computed (zero).  A request wider than half a batch runs as
+ * consecutive pieces of at most half a batch, interleaved with other requests'
+ * batches, and its result is merged from theirs; any range with b up to
+ * 10^14 + 10^10 + 1 is accepted. */
 #define VOSS_OP_COUNT      0
 #define VOSS_OP_TWINS      1
 #define VOSS_OP_GAP_HIST   2
